@@ -1,0 +1,319 @@
+"""Ray-tracing throughput on one GB300 (Mrays/s).
+
+Workload (default): the 1.31M-triangle displaced icosphere (20 faces
+subdivided 8 times, radius 1, radial value-noise displacement 0.05), SAH kd
+tree (traversal cost 1, intersection cost 1.5), 1920x1080, one primary ray per
+pixel plus one occlusion ray per light (2 point lights) where the light is in
+front of the surface. det threshold 0 (the reference's 1e-4 culls every
+triangle of this sphere). One step = one frame rendered by the
+fused ray-tracing kernel with the scene resident in HBM.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0). Under torchrun every rank renders its own frames
+on its own GPU (replicas; the path does not exchange data), value = all ranks'
+rays / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
+PARAM_BLOCK_BYTES = 1676     # kernel parameter block of one render launch (camera, lights, pointers)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["icosphere", "soup"], default="icosphere")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    return ap.parse_args()
+
+
+def workload(name):
+    from nostrum_pray_gb300 import scenes
+    if name == "icosphere":
+        mesh = scenes.icosphere(8)
+        setup = scenes.icosphere_setup(1920, 1080, det_eps=0.0)
+        cfg = {"workload": "displaced icosphere 1,310,720 triangles, SAH kd tree (Ct 1, Ci 1.5), 1920x1080, "
+                           "1 primary + up to 2 occlusion rays per pixel, det threshold 0",
+               "triangles": mesh.n, "width": 1920, "height": 1080, "lights": 2, "tree": "sah",
+               "det_epsilon": 0.0}
+    else:
+        mesh = scenes.soup(10_000, 0)
+        setup = scenes.soup_setup()
+        cfg = {"workload": "triangle soup 10,000 triangles, median kd tree (leaf 8, depth 24), 512x512, "
+                           "1 primary + 1 occlusion ray per pixel, det threshold 1e-4",
+               "triangles": mesh.n, "width": 512, "height": 512, "lights": 1, "tree": "median",
+               "det_epsilon": 1e-4}
+    return mesh, setup, cfg
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples of one GPU during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = os.path.join("/tmp", f"pray_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic(kernel: str, workload_name: str):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}_{workload_name}.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f).get("dram_bytes_per_launch")
+    return None
+
+
+def cpu_baseline(mesh, setup, budget_s: float, threads=None):
+    """The oracle's restatement of the reference's tracer (full depth-first
+    traversal, scalar Moeller-Trumbore, OpenMP over rows) on a bounded sample of
+    central image rows. Returns (Mrays/s, cores, sample description)."""
+    from oracle import oracle as O
+    O.build()
+    orc = O.OracleScene.from_setup(mesh, setup)
+    thr = threads or O.default_threads()
+    mid = setup.height // 2
+    rows, rays, elapsed = 0, 0, 0.0
+    chunk = 8
+    lo = hi = mid
+    while elapsed < budget_s and (lo > 0 or hi < setup.height):
+        a, b = max(0, lo - chunk // 2), min(setup.height, hi + chunk // 2)
+        for r0, r1 in ((a, lo), (hi, b)):
+            if r1 <= r0:
+                continue
+            t0 = time.perf_counter()
+            _, nsh = orc.render_rt(setup, rows=(r0, r1), threads=thr)
+            elapsed += time.perf_counter() - t0
+            rays += (r1 - r0) * setup.width + nsh
+            rows += r1 - r0
+        lo, hi = a, b
+    return rays / elapsed / 1e6, thr, f"{rows} central rows of {setup.height} ({rows * setup.width} pixels, " \
+                                      f"{rays} rays) in {elapsed:.1f} s"
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    mesh, setup, cfg = workload(args.workload)
+    from oracle import oracle as O
+    O.build()
+    orc = O.OracleScene.from_setup(mesh, setup)
+    thr = O.default_threads()
+    rows = 24
+    r0 = setup.height // 2 - rows // 2
+    def step():
+        t0 = time.perf_counter()
+        _, nsh = orc.render_rt(setup, rows=(r0, r0 + rows), threads=thr)
+        return time.perf_counter() - t0, rows * setup.width + nsh
+    for _ in range(args.warmup):
+        step()
+    total_t, total_r = 0.0, 0
+    for _ in range(args.steps):
+        t, r = step()
+        total_t += t
+        total_r += r
+    v = total_r / total_t / 1e6
+    sample = f"each step: {rows} central rows x {setup.width} pixels with their occlusion rays"
+    line = {"impl": "reference", "metric": "Mrays/s", "value": round(v, 4), "unit": "Mrays/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 * total_t / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+            "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": thr, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(v, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "CPU restatement of the reference's scalar tracer (oracle/pray_oracle.cpp); the reference's "
+                    "own x86 AVX build does not run on this host"}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+    from nostrum_pray_gb300 import native
+    try:
+        native.lib()
+    except native.PrayError:
+        from nostrum_pray_gb300 import build
+        build.build()
+    mesh, setup, cfg = workload(args.workload)
+    t0 = time.perf_counter()
+    sc = native.Scene.from_setup(mesh, setup, device=dev)
+    build_s = time.perf_counter() - t0
+    h, w = setup.height, setup.width
+    rgb = torch.empty((h, w, 3), dtype=torch.uint8, device="cuda")
+    cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    counts = sc.render_rt_counts(setup)  # [primary, occlusion, pair fetches, tri fetches, shaded hits]
+    rays_per_frame = int(counts[0] + counts[1])
+    for _ in range(args.warmup):
+        sc.render_rt(setup, rgb, counters=cnt)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(dev) if rank == 0 else None
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()  # evict the scene from L2 between frames
+        starts[k].record(stream)
+        sc.render_rt(setup, rgb, stream=stream)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    wall = time.perf_counter() - wall0
+    clocks = sampler.stop() if sampler else None
+    times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    kernel_ms = sum(times)
+    t_local = torch.tensor([kernel_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t_local, op=torch.distributed.ReduceOp.MAX)
+    kernel_ms_max = float(t_local.item())
+    value = rays_per_frame * args.steps * world / (kernel_ms_max / 1e3) / 1e6
+
+    # end to end through the host-memory C ABI entry point (params in, image out)
+    for _ in range(2):
+        sc.render_rt_host(setup)
+    e2e_times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        img, _ = sc.render_rt_host(setup)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_val = rays_per_frame * world / statistics.mean(e2e_times) / 1e6
+
+    # roofline of the render kernel: algorithmic bytes per launch
+    prim, occl, pairs, tris, hits = (int(x) for x in counts)
+    alg_bytes = 32 * (prim + occl) + 64 * pairs + 48 * tris + 32 * hits + 3 * w * h
+    mean_s = kernel_ms / args.steps / 1e3
+    achieved = alg_bytes / mean_s / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = committed_traffic("k_render_rt", args.workload)
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        v, cores, sample = cpu_baseline(mesh, setup, args.cpu_seconds)
+        cpu = {"value": round(v, 4), "unit": "Mrays/s", "cores": cores, "kind": "port", "sample": sample}
+    cfg = dict(cfg)
+    cfg.update({"parallelism": f"replicas x{world}", "l2": "flushed between steps (256 MB write)",
+                "tree_build_s": round(build_s, 2), "rays_per_frame": rays_per_frame})
+    line = {"metric": "Mrays/s", "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(kernel_ms_max / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": cfg,
+            "e2e": {"value": round(e2e_val, 2), "unit": "Mrays/s", "h2d_bytes_per_step": PARAM_BLOCK_BYTES,
+                    "d2h_bytes_per_step": 3 * w * h + 16},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": traffic,
+                         "peak_kind": f"{peak_kind} HBM copy bandwidth",
+                         "algorithmic_bytes_per_launch": alg_bytes,
+                         "counts": {"primary": prim, "occlusion": occl, "node_pair_fetches": pairs,
+                                    "triangle_fetches": tris, "shaded_hits": hits}},
+            "wall_s_timed_loop": round(wall, 4), "clocks": clocks, "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,177 @@
+/*
+ * nostrum_pray GB300 — C ABI of the ray-tracing hot path.
+ *
+ * Plain pointers and sizes only. Every function returns a pray_status; on an
+ * error pray_last_error() gives a message (per calling thread). No function
+ * exits the process (the reference does so inside library code:
+ * src/io.cpp:33,57 and src/path_trace.cu:15).
+ *
+ * Threading: a pray_scene is not thread-safe; the caller serialises calls on
+ * one handle. Different handles are independent. Device-pointer entry points
+ * enqueue work on the given CUDA stream (NULL: the legacy default stream) and
+ * do not synchronise; *_host entry points synchronise before returning.
+ *
+ * Reference interfaces replaced (paths in the reference project):
+ *   SpatialDatabase::build / KDTree / KDTreeSAH   include/spatial.h:10-39,
+ *                                                  src/kd_tree.cpp:18-84,
+ *                                                  src/kd_tree_sah.cpp:25-138
+ *   SpatialDatabase::intersect (per ray)           include/spatial.h:16,
+ *                                                  src/kd_tree.cpp:142-279
+ *   render / rayTrace                              include/pray.h:50-53,
+ *                                                  src/pray.cpp:380-637
+ */
+#ifndef NOSTRUM_PRAY_H
+#define NOSTRUM_PRAY_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PRAY_API_VERSION 1
+
+typedef enum {
+    PRAY_OK = 0,
+    PRAY_ERR_INVALID_ARGUMENT = 1,
+    PRAY_ERR_CUDA = 2,
+    PRAY_ERR_OUT_OF_MEMORY = 3,
+    PRAY_ERR_IO = 4,
+    PRAY_ERR_UNSUPPORTED = 5
+} pray_status;
+
+typedef enum { PRAY_TREE_MEDIAN = 0, PRAY_TREE_SAH = 1 } pray_tree_kind;
+
+/* Tree construction constants. The reference fixes them at compile time
+ * (include/kd_tree.h:50-52, include/kd_tree_sah.h:49-50); here they are
+ * arguments. pray_tree_options_default() fills the reference's values. */
+typedef struct {
+    int32_t tree;                  /* pray_tree_kind */
+    int32_t leaf_size;             /* THRESHOLD: leaf at <= this many triangles (32) */
+    int32_t max_depth;             /* MAX_DEPTH: leaf at this depth (20); at most 30 */
+    float sah_traversal_cost;      /* traversalCost (5) */
+    float sah_intersection_cost;   /* triangleIntersectionCost (1.5) */
+    int32_t build_threads;         /* host threads for the build, 0 = all */
+} pray_tree_options;
+
+/* Ray-tracing frame parameters: the scene JSON's camera, lights and
+ * background (src/io.cpp:60-101) plus the intersector's det threshold
+ * (include/geometry.h:12, EPSILON = 1e-4 in the reference). */
+typedef struct {
+    uint64_t width, height;
+    uint64_t fov;                  /* degrees, horizontal */
+    float camera_position[3];
+    float camera_look[3];
+    float background[3];
+    const float *lights;           /* host memory: n_lights x (position[3], colour[3]) */
+    int32_t n_lights;              /* at most 64 */
+    float det_epsilon;
+} pray_rt_params;
+
+/* Path-tracing frame parameters (scene JSON "method": "path_tracing",
+ * src/io.cpp:60-63). */
+typedef enum {
+    PRAY_PT_KAJIYA = 0,   /* the reference's evaluatePathRecursive (src/pray.cpp:342-364) */
+    PRAY_PT_NEE = 1       /* next-event estimation + Russian roulette (no reference counterpart) */
+} pray_pt_mode;
+
+typedef struct {
+    uint64_t width, height;
+    uint64_t fov;
+    float camera_position[3];
+    float camera_look[3];
+    float background[3];
+    uint32_t max_depth;            /* bounces: a hit at depth >= max_depth returns 0 */
+    uint32_t num_samples;          /* paths per pixel */
+    uint64_t seed;                 /* PCG32 streams per (seed, pixel, sample) */
+    float det_epsilon;
+    int32_t mode;                  /* pray_pt_mode */
+    uint32_t rr_depth;             /* PRAY_PT_NEE: Russian roulette from this depth */
+} pray_pt_params;
+
+typedef struct pray_scene pray_scene;
+typedef struct pray_host_tree pray_host_tree;
+
+const char *pray_last_error(void);
+int32_t pray_api_version(void);
+void pray_tree_options_default(pray_tree_options *opt);
+
+/* ---- host-only tree build (no device work; for inspection and tests) ---- */
+
+/* Precompute (initialiseTriangles, src/scene_preprocessor.cpp:74-96) and build
+ * the tree. verts: n x 9 floats (a, b, c). */
+pray_status pray_host_tree_build(const float *verts, uint64_t n, const pray_tree_options *opt,
+                                 pray_host_tree **out);
+void pray_host_tree_destroy(pray_host_tree *t);
+/* out[5] = nodes, max depth, leaf nodes, empty leaf nodes, leaf references */
+pray_status pray_host_tree_stats(const pray_host_tree *t, uint64_t *out);
+/* Depth-first pre-order dump (left before right): per node box[6] (min, max),
+ * split distance, info[4] = {is_leaf, split axis (255 for leaves), triangle
+ * count, first reference}; refs = leaf triangle indices in DFS order. Array
+ * sizes from pray_host_tree_stats. */
+pray_status pray_host_tree_dump(const pray_host_tree *t, float *boxes, float *split, int32_t *info,
+                                int64_t *refs);
+/* Per triangle: box min[3], box max[3], midpoint[3], b-a[3], c-a[3], normal[3]. */
+pray_status pray_host_tree_precompute(const pray_host_tree *t, float *out18);
+
+/* Camera constants the kernels use: inverse view matrix rows 0-2 (columns
+ * 0-2), 1/width, 1/height, aspect, tan(fov/2) — 13 floats
+ * (calculatePrimRays set-up, src/scene_preprocessor.cpp:98-120). */
+pray_status pray_camera(uint64_t width, uint64_t height, uint64_t fov, const float *camera_position,
+                        const float *camera_look, float *out13);
+
+/* ---- device scenes ---- */
+
+/* Builds the tree on the host and uploads nodes, triangle references and
+ * shading data to `device`. The caller keeps its buffers. colors: n x 3
+ * (albedo, or radiance when emit[i] != 0); emit may be NULL. */
+pray_status pray_scene_create(const float *verts, const float *colors, const uint8_t *emit, uint64_t n,
+                              const pray_tree_options *opt, int32_t device, pray_scene **out);
+pray_status pray_scene_destroy(pray_scene *s);
+/* out[8] = nodes, max depth, leaf nodes, empty leaf nodes, leaf references,
+ *          triangles, device bytes held, device node records */
+pray_status pray_scene_stats(const pray_scene *s, uint64_t *out);
+
+/* Closest hit per ray (SpatialDatabase::intersect). rays_dev: n x 9 floats
+ * (position, unit direction, 1/direction — the reference's Ray fields), all
+ * device pointers. ids_dev: triangle index or -1; t_dev: distance, FLT_MAX on
+ * a miss. Same triangle and distance as the reference's depth-first
+ * traversal, ties included. */
+pray_status pray_trace_closest(pray_scene *s, const float *rays_dev, uint64_t n, float det_epsilon,
+                               int32_t *ids_dev, float *t_dev, void *stream);
+
+/* One ray-traced frame into device memory: rgb_dev height x width x 3 bytes,
+ * top row first (the reference's Image layout). ids_dev / t_dev (per pixel,
+ * may be NULL) receive the primary hits. counters_dev (may be NULL) is
+ * incremented by [primary rays, occlusion rays]. */
+pray_status pray_render_rt(pray_scene *s, const pray_rt_params *p, uint8_t *rgb_dev, int32_t *ids_dev,
+                           float *t_dev, unsigned long long *counters_dev, void *stream);
+
+/* The same frame into host memory (render(Image&, const Scene&) of
+ * include/pray.h:50): rgb_host height x width x 3 bytes. rays_cast (may be
+ * NULL) receives [primary rays, occlusion rays]. Synchronises. */
+pray_status pray_render_rt_host(pray_scene *s, const pray_rt_params *p, uint8_t *rgb_host,
+                                uint64_t *rays_cast);
+
+/* Work counts of one ray-traced frame, from an instrumented run of the same
+ * kernel: out[5] = primary rays, occlusion rays, node-pair fetches (64 bytes
+ * each), triangle-reference fetches (48 bytes each), shaded hits. */
+pray_status pray_render_rt_counts(pray_scene *s, const pray_rt_params *p, uint64_t *out);
+
+/* One path-traced frame (pathTrace, src/pray.cpp:592-615) into device
+ * memory: rgb_dev as for pray_render_rt; radiance_dev (may be NULL) receives
+ * the per-pixel mean radiance (height x width x 3 floats) before clamping;
+ * counters_dev (may be NULL) is incremented by [paths, ray segments]. */
+pray_status pray_render_pt(pray_scene *s, const pray_pt_params *p, uint8_t *rgb_dev, float *radiance_dev,
+                           unsigned long long *counters_dev, void *stream);
+
+/* The same into host memory; radiance_host and rays_cast ([paths, segments])
+ * may be NULL. Synchronises. */
+pray_status pray_render_pt_host(pray_scene *s, const pray_pt_params *p, uint8_t *rgb_host, float *radiance_host,
+                                uint64_t *rays_cast);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NOSTRUM_PRAY_H */

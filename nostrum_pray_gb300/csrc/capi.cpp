@@ -1,0 +1,576 @@
+// C-ABI entry points (include/nostrum_pray.h): scene build and upload, error
+// reporting, and the tracing launches.
+#include "../../include/nostrum_pray.h"
+
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "capi_internal.h"
+#include "device_layout.h"
+#include "host/camera.h"
+#include "host/kdtree.h"
+#include "trace_launch.h"
+
+using namespace pray_gpu;
+
+namespace {
+
+thread_local std::string g_error;
+
+}  // namespace
+
+namespace pray_gpu {
+
+pray_status set_error(pray_status st, const std::string &msg) {
+    g_error = msg;
+    return st;
+}
+
+pray_status cuda_error(cudaError_t e, const char *what) {
+    return set_error(e == cudaErrorMemoryAllocation ? PRAY_ERR_OUT_OF_MEMORY : PRAY_ERR_CUDA,
+                     std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bool valid_options(const pray_tree_options *opt, std::string &why) {
+    if (opt->tree != PRAY_TREE_MEDIAN && opt->tree != PRAY_TREE_SAH) {
+        why = "tree must be PRAY_TREE_MEDIAN or PRAY_TREE_SAH";
+        return false;
+    }
+    if (opt->leaf_size < 1) {
+        why = "leaf_size must be >= 1";
+        return false;
+    }
+    if (opt->max_depth < 0 || opt->max_depth > kMaxTreeDepth) {
+        why = "max_depth must be in [0, 30]";
+        return false;
+    }
+    if (!(opt->sah_traversal_cost >= 0.f) || !(opt->sah_intersection_cost > 0.f)) {
+        why = "SAH costs must be finite, traversal >= 0 and intersection > 0";
+        return false;
+    }
+    return true;
+}
+
+TreeOptions to_options(const pray_tree_options *opt) {
+    TreeOptions o;
+    o.kind = opt->tree;
+    o.leaf_size = opt->leaf_size;
+    o.max_depth = opt->max_depth;
+    o.sah_ct = opt->sah_traversal_cost;
+    o.sah_ci = opt->sah_intersection_cost;
+    o.threads = opt->build_threads;
+    return o;
+}
+
+// Flattening into sibling-pair nodes; refs keep their DFS order.
+void flatten_device(const BuiltTree &t, std::vector<GNode> &out) {
+    out.assign(2, GNode{});
+    struct Rec {
+        static void put(const BuiltTree &t, int32_t p, uint32_t slot, std::vector<GNode> &out) {
+            const FlatNode &n = t.nodes[p];
+            GNode g;
+            for (int k = 0; k < 3; k++) g.lo[k] = n.box.lo[k], g.hi[k] = n.box.hi[k];
+            if (n.left < 0) {
+                g.a = n.first;
+                g.b = kLeafFlag | n.count;
+                out[slot] = g;
+                return;
+            }
+            const uint32_t pair = (uint32_t)out.size();
+            out.resize(out.size() + 2);
+            g.a = pair;
+            g.b = 0;
+            out[slot] = g;
+            put(t, n.left, pair, out);
+            put(t, n.right, pair + 1, out);
+        }
+    };
+    Rec::put(t, 0, 0, out);
+}
+
+}  // namespace pray_gpu
+
+struct pray_host_tree {
+    std::vector<TriPre> tris;
+    BuiltTree tree;
+};
+
+struct pray_scene {
+    int device = 0;
+    uint64_t n_tris = 0;
+    BuiltTree tree;  // host copy (statistics, dumps)
+    GNode *d_nodes = nullptr;
+    GTri *d_tris = nullptr;
+    GShade *d_shade = nullptr;
+    GTri *d_emit = nullptr;
+    float *d_emit_cdf = nullptr;
+    uint32_t n_emit = 0;
+    float emit_area = 0.f;
+    uint32_t n_gnodes = 0;
+    float tol = 0.f;
+    uint64_t device_bytes = 0;
+    // frame buffers of the host-memory entry points, grown on demand
+    uint8_t *d_rgb = nullptr;
+    uint64_t rgb_cap = 0;
+    unsigned long long *d_counters = nullptr;
+
+    DevScene view() const {
+        DevScene v;
+        v.nodes = d_nodes;
+        v.tris = d_tris;
+        v.shade = d_shade;
+        v.n_nodes = n_gnodes;
+        v.n_refs = (uint32_t)tree.refs.size();
+        v.n_tris = (uint32_t)n_tris;
+        v.tol = tol;
+        v.emit_tris = d_emit;
+        v.emit_cdf = d_emit_cdf;
+        v.n_emit = n_emit;
+        v.emit_area = emit_area;
+        return v;
+    }
+    void release() {
+        cudaFree(d_nodes);
+        cudaFree(d_tris);
+        cudaFree(d_shade);
+        cudaFree(d_rgb);
+        cudaFree(d_counters);
+        cudaFree(d_emit);
+        cudaFree(d_emit_cdf);
+        d_nodes = nullptr, d_tris = nullptr, d_shade = nullptr, d_rgb = nullptr, d_counters = nullptr;
+        d_emit = nullptr, d_emit_cdf = nullptr;
+    }
+};
+
+namespace {
+
+#define PRAY_TRY(...)                                                           \
+    try {                                                                       \
+        __VA_ARGS__                                                             \
+    } catch (const std::bad_alloc &) {                                          \
+        return set_error(PRAY_ERR_OUT_OF_MEMORY, "host allocation failed");     \
+    } catch (const std::exception &e) {                                         \
+        return set_error(PRAY_ERR_INVALID_ARGUMENT, e.what());                  \
+    }
+
+void dump_tree(const BuiltTree &t, float *boxes, float *split, int32_t *info, int64_t *refs) {
+    for (size_t i = 0; i < t.nodes.size(); i++) {
+        const FlatNode &n = t.nodes[i];
+        for (int k = 0; k < 3; k++) boxes[6 * i + k] = n.box.lo[k], boxes[6 * i + 3 + k] = n.box.hi[k];
+        split[i] = n.split;
+        const bool leaf = n.left < 0;
+        info[4 * i] = leaf ? 1 : 0;
+        info[4 * i + 1] = n.axis;
+        info[4 * i + 2] = leaf ? (int32_t)n.count : 0;
+        info[4 * i + 3] = (int32_t)n.first;
+    }
+    for (size_t i = 0; i < t.refs.size(); i++) refs[i] = t.refs[i];
+}
+
+void tree_stats(const BuiltTree &t, uint64_t *out) {
+    out[0] = t.nodes.size();
+    out[1] = t.maxdepth;
+    out[2] = t.leaf_nodes;
+    out[3] = t.empty_leaves;
+    out[4] = t.refs.size();
+}
+
+pray_status check_params(const pray_rt_params *p) {
+    if (!p) return set_error(PRAY_ERR_INVALID_ARGUMENT, "params is NULL");
+    if (p->width == 0 || p->height == 0 || p->width > 65536 || p->height > 65536)
+        return set_error(PRAY_ERR_INVALID_ARGUMENT, "width and height must be in [1, 65536]");
+    if (p->n_lights < 0 || p->n_lights > kMaxLights)
+        return set_error(PRAY_ERR_INVALID_ARGUMENT, "n_lights must be in [0, 64]");
+    if (p->n_lights > 0 && !p->lights) return set_error(PRAY_ERR_INVALID_ARGUMENT, "lights is NULL");
+    return PRAY_OK;
+}
+
+pray_status check_pt_params(const pray_pt_params *p) {
+    if (!p) return set_error(PRAY_ERR_INVALID_ARGUMENT, "params is NULL");
+    if (p->width == 0 || p->height == 0 || p->width > 65536 || p->height > 65536)
+        return set_error(PRAY_ERR_INVALID_ARGUMENT, "width and height must be in [1, 65536]");
+    if (p->num_samples == 0) return set_error(PRAY_ERR_INVALID_ARGUMENT, "num_samples must be >= 1");
+    if (p->max_depth >= (uint32_t)kMaxPtDepth)
+        return set_error(PRAY_ERR_UNSUPPORTED, "max_depth must be below 64");
+    if (p->mode != PRAY_PT_KAJIYA && p->mode != PRAY_PT_NEE)
+        return set_error(PRAY_ERR_INVALID_ARGUMENT, "mode must be PRAY_PT_KAJIYA or PRAY_PT_NEE");
+    return PRAY_OK;
+}
+
+PtLaunch make_pt_launch(const pray_pt_params *p) {
+    PtLaunch L;
+    std::memset(&L, 0, sizeof(L));
+    L.cam = make_camera(p->width, p->height, p->fov, p->camera_position, p->camera_look);
+    for (int k = 0; k < 3; k++) L.bg[k] = p->background[k];
+    L.max_depth = p->max_depth;
+    L.num_samples = p->num_samples;
+    L.rr_depth = p->rr_depth;
+    L.mode = p->mode;
+    L.seed = p->seed;
+    L.eps = p->det_epsilon;
+    return L;
+}
+
+RtLaunch make_launch(const pray_rt_params *p) {
+    RtLaunch L;
+    std::memset(&L, 0, sizeof(L));
+    L.cam = make_camera(p->width, p->height, p->fov, p->camera_position, p->camera_look);
+    L.n_lights = p->n_lights;
+    for (int i = 0; i < p->n_lights; i++)
+        for (int k = 0; k < 6; k++) L.lights[i][k] = p->lights[6 * i + k];
+    for (int k = 0; k < 3; k++) L.bg[k] = p->background[k];
+    L.eps = p->det_epsilon;
+    return L;
+}
+
+}  // namespace
+
+// Grows the frame buffer of the host-memory entry points to `bytes` (plus
+// alignment slack) and makes sure the ray counters exist.
+pray_status ensure_frame(pray_scene *s, uint64_t bytes) {
+    cudaError_t e;
+    bytes += 16;
+    if (bytes > s->rgb_cap) {
+        cudaFree(s->d_rgb);
+        s->d_rgb = nullptr;
+        s->rgb_cap = 0;
+        if ((e = cudaMalloc(&s->d_rgb, bytes)) != cudaSuccess) return cuda_error(e, "cudaMalloc (frame)");
+        s->rgb_cap = bytes;
+    }
+    if (!s->d_counters && (e = cudaMalloc(&s->d_counters, 8 * sizeof(unsigned long long))) != cudaSuccess)
+        return cuda_error(e, "cudaMalloc (counters)");
+    return PRAY_OK;
+}
+
+extern "C" {
+
+const char *pray_last_error(void) { return g_error.c_str(); }
+
+int32_t pray_api_version(void) { return PRAY_API_VERSION; }
+
+void pray_tree_options_default(pray_tree_options *opt) {
+    if (!opt) return;
+    opt->tree = PRAY_TREE_MEDIAN;
+    opt->leaf_size = 32;
+    opt->max_depth = 20;
+    opt->sah_traversal_cost = 5.f;
+    opt->sah_intersection_cost = 1.5f;
+    opt->build_threads = 0;
+}
+
+pray_status pray_host_tree_build(const float *verts, uint64_t n, const pray_tree_options *opt,
+                                 pray_host_tree **out) {
+    if (!out || !opt || (n > 0 && !verts)) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n >= (1ull << 31)) return set_error(PRAY_ERR_INVALID_ARGUMENT, "too many triangles (max 2^31-1)");
+    std::string why;
+    if (!valid_options(opt, why)) return set_error(PRAY_ERR_INVALID_ARGUMENT, why);
+    PRAY_TRY({
+        auto t = std::make_unique<pray_host_tree>();
+        t->tris = precompute_triangles(verts, n, opt->build_threads);
+        t->tree = build_tree(t->tris, to_options(opt));
+        *out = t.release();
+        return PRAY_OK;
+    })
+}
+
+void pray_host_tree_destroy(pray_host_tree *t) { delete t; }
+
+pray_status pray_host_tree_stats(const pray_host_tree *t, uint64_t *out) {
+    if (!t || !out) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    tree_stats(t->tree, out);
+    return PRAY_OK;
+}
+
+pray_status pray_host_tree_dump(const pray_host_tree *t, float *boxes, float *split, int32_t *info,
+                                int64_t *refs) {
+    if (!t || !boxes || !split || !info || !refs) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    dump_tree(t->tree, boxes, split, info, refs);
+    return PRAY_OK;
+}
+
+pray_status pray_host_tree_precompute(const pray_host_tree *t, float *out) {
+    if (!t || !out) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    for (size_t i = 0; i < t->tris.size(); i++) {
+        const TriPre &p = t->tris[i];
+        const F3 *vs[6] = {&p.box.lo, &p.box.hi, &p.mid, &p.ab, &p.ac, &p.normal};
+        for (int k = 0; k < 6; k++)
+            for (int c = 0; c < 3; c++) out[18 * i + 3 * k + c] = (*vs[k])[c];
+    }
+    return PRAY_OK;
+}
+
+pray_status pray_camera(uint64_t width, uint64_t height, uint64_t fov, const float *pos, const float *look,
+                        float *out) {
+    if (!pos || !look || !out) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (width == 0 || height == 0) return set_error(PRAY_ERR_INVALID_ARGUMENT, "empty image");
+    CameraConsts c = make_camera(width, height, fov, pos, look);
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) out[3 * i + j] = c.m[i][j];
+    out[9] = c.inv_w;
+    out[10] = c.inv_h;
+    out[11] = c.aspect;
+    out[12] = c.angle;
+    return PRAY_OK;
+}
+
+pray_status pray_scene_create(const float *verts, const float *colors, const uint8_t *emit, uint64_t n,
+                              const pray_tree_options *opt, int32_t device, pray_scene **out) {
+    if (!out || !opt || (n > 0 && (!verts || !colors))) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n >= (1ull << 31)) return set_error(PRAY_ERR_INVALID_ARGUMENT, "too many triangles (max 2^31-1)");
+    std::string why;
+    if (!valid_options(opt, why)) return set_error(PRAY_ERR_INVALID_ARGUMENT, why);
+    *out = nullptr;
+    std::unique_ptr<pray_scene> s;
+    std::vector<TriPre> pre;
+    std::vector<GNode> gnodes;
+    std::vector<GTri> gtris;
+    std::vector<GShade> gshade;
+    std::vector<GTri> gemit;
+    std::vector<float> gcdf;
+    PRAY_TRY({
+        s = std::make_unique<pray_scene>();
+        s->device = device;
+        s->n_tris = n;
+        pre = precompute_triangles(verts, n, opt->build_threads);
+        s->tree = build_tree(pre, to_options(opt));
+        if (s->tree.refs.size() >= (1ull << 31))
+            return set_error(PRAY_ERR_UNSUPPORTED, "more than 2^31-1 leaf references");
+        flatten_device(s->tree, gnodes);
+        gtris.resize(s->tree.refs.size());
+        for (size_t i = 0; i < s->tree.refs.size(); i++) {
+            const uint32_t id = s->tree.refs[i];
+            const TriPre &p = pre[id];
+            GTri &g = gtris[i];
+            uint32_t idbits = id;
+            float idf;
+            std::memcpy(&idf, &idbits, 4);
+            g.v0[0] = p.a[0], g.v0[1] = p.a[1], g.v0[2] = p.a[2], g.v0[3] = idf;
+            g.e1[0] = p.ab[0], g.e1[1] = p.ab[1], g.e1[2] = p.ab[2], g.e1[3] = 0.f;
+            g.e2[0] = p.ac[0], g.e2[1] = p.ac[1], g.e2[2] = p.ac[2], g.e2[3] = 0.f;
+        }
+        gshade.resize(n);
+        for (uint64_t i = 0; i < n; i++) {
+            GShade &g = gshade[i];
+            for (int k = 0; k < 3; k++) g.n[k] = pre[i].normal[k], g.c[k] = colors[3 * i + k];
+            g.n[3] = (emit && emit[i]) ? 1.f : 0.f;
+            g.c[3] = 0.f;
+        }
+        // emitters for next-event estimation: geometry and area prefix sums
+        // (area = |ab x ac| / 2 in double, summed in double)
+        double acc = 0.0;
+        for (uint64_t i = 0; i < n; i++) {
+            if (!(emit && emit[i])) continue;
+            const TriPre &p = pre[i];
+            const F3 c = cross3(p.ab, p.ac);
+            const double area = 0.5 * std::sqrt((double)c[0] * c[0] + (double)c[1] * c[1] + (double)c[2] * c[2]);
+            if (!(area > 0.0)) continue;
+            acc += area;
+            GTri g;
+            uint32_t idbits = (uint32_t)i;
+            float idf;
+            std::memcpy(&idf, &idbits, 4);
+            g.v0[0] = p.a[0], g.v0[1] = p.a[1], g.v0[2] = p.a[2], g.v0[3] = idf;
+            g.e1[0] = p.ab[0], g.e1[1] = p.ab[1], g.e1[2] = p.ab[2], g.e1[3] = 0.f;
+            g.e2[0] = p.ac[0], g.e2[1] = p.ac[1], g.e2[2] = p.ac[2], g.e2[3] = 0.f;
+            gemit.push_back(g);
+            gcdf.push_back((float)acc);
+        }
+        s->emit_area = gcdf.empty() ? 0.f : gcdf.back();
+        // box-behind-origin margin: 1e-5 of the scene's diagonal
+        const Aabb &rb = s->tree.nodes[0].box;
+        float diag = 0.f;
+        if (n > 0) {
+            for (int k = 0; k < 3; k++) {
+                const float e = rb.hi[k] - rb.lo[k];
+                diag += e * e;
+            }
+            diag = std::sqrt(diag);
+        }
+        s->tol = std::isfinite(diag) ? diag * 1e-5f : FLT_MAX;
+    })
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    const size_t nb = gnodes.size() * sizeof(GNode), tb = std::max<size_t>(gtris.size(), 1) * sizeof(GTri),
+                 sb = std::max<size_t>(gshade.size(), 1) * sizeof(GShade);
+    if ((e = cudaMalloc(&s->d_nodes, nb)) != cudaSuccess || (e = cudaMalloc(&s->d_tris, tb)) != cudaSuccess ||
+        (e = cudaMalloc(&s->d_shade, sb)) != cudaSuccess) {
+        s->release();
+        return cuda_error(e, "cudaMalloc (scene)");
+    }
+    if ((e = cudaMemcpy(s->d_nodes, gnodes.data(), nb, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (!gtris.empty() &&
+         (e = cudaMemcpy(s->d_tris, gtris.data(), gtris.size() * sizeof(GTri), cudaMemcpyHostToDevice)) !=
+             cudaSuccess) ||
+        (!gshade.empty() && (e = cudaMemcpy(s->d_shade, gshade.data(), gshade.size() * sizeof(GShade),
+                                            cudaMemcpyHostToDevice)) != cudaSuccess)) {
+        s->release();
+        return cuda_error(e, "cudaMemcpy (scene upload)");
+    }
+    if (!gemit.empty()) {
+        if ((e = cudaMalloc(&s->d_emit, gemit.size() * sizeof(GTri))) != cudaSuccess ||
+            (e = cudaMalloc(&s->d_emit_cdf, gcdf.size() * sizeof(float))) != cudaSuccess ||
+            (e = cudaMemcpy(s->d_emit, gemit.data(), gemit.size() * sizeof(GTri), cudaMemcpyHostToDevice)) !=
+                cudaSuccess ||
+            (e = cudaMemcpy(s->d_emit_cdf, gcdf.data(), gcdf.size() * sizeof(float), cudaMemcpyHostToDevice)) !=
+                cudaSuccess) {
+            s->release();
+            return cuda_error(e, "emitter upload");
+        }
+        s->n_emit = (uint32_t)gemit.size();
+    }
+    s->n_gnodes = (uint32_t)gnodes.size();
+    s->device_bytes = nb + tb + sb + gemit.size() * (sizeof(GTri) + sizeof(float));
+    *out = s.release();
+    return PRAY_OK;
+}
+
+pray_status pray_scene_destroy(pray_scene *s) {
+    if (!s) return PRAY_OK;
+    cudaSetDevice(s->device);
+    s->release();
+    delete s;
+    return PRAY_OK;
+}
+
+pray_status pray_scene_stats(const pray_scene *s, uint64_t *out) {
+    if (!s || !out) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    tree_stats(s->tree, out);
+    out[5] = s->n_tris;
+    out[6] = s->device_bytes;
+    out[7] = s->n_gnodes;
+    return PRAY_OK;
+}
+
+pray_status pray_trace_closest(pray_scene *s, const float *rays, uint64_t n, float eps, int32_t *ids, float *ts,
+                               void *stream) {
+    if (!s || (n > 0 && (!rays || !ids || !ts))) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n >= (1ull << 40)) return set_error(PRAY_ERR_INVALID_ARGUMENT, "too many rays");
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    e = launch_trace_closest(s->view(), rays, n, eps, ids, ts, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_error(e, "trace_closest launch");
+    return PRAY_OK;
+}
+
+pray_status pray_render_rt(pray_scene *s, const pray_rt_params *p, uint8_t *rgb, int32_t *ids, float *ts,
+                           unsigned long long *counters, void *stream) {
+    if (!s || !rgb) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    if ((ids == nullptr) != (ts == nullptr))
+        return set_error(PRAY_ERR_INVALID_ARGUMENT, "ids and t must both be given or both be NULL");
+    pray_status st = check_params(p);
+    if (st != PRAY_OK) return st;
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    RtLaunch L = make_launch(p);
+    L.rgb = rgb;
+    L.ids = ids;
+    L.ts = ts;
+    L.counters = counters;
+    e = launch_render_rt(s->view(), L, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_error(e, "render_rt launch");
+    return PRAY_OK;
+}
+
+pray_status pray_render_rt_host(pray_scene *s, const pray_rt_params *p, uint8_t *rgb_host, uint64_t *rays_cast) {
+    if (!s || !rgb_host) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    pray_status st = check_params(p);
+    if (st != PRAY_OK) return st;
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    const uint64_t bytes = 3ull * p->width * p->height;
+    if ((st = ensure_frame(s, bytes)) != PRAY_OK) return st;
+    if ((e = cudaMemsetAsync(s->d_counters, 0, 2 * sizeof(unsigned long long), 0)) != cudaSuccess)
+        return cuda_error(e, "cudaMemsetAsync");
+    RtLaunch L = make_launch(p);
+    L.rgb = s->d_rgb;
+    L.counters = s->d_counters;
+    if ((e = launch_render_rt(s->view(), L, 0)) != cudaSuccess) return cuda_error(e, "render_rt launch");
+    if ((e = cudaMemcpy(rgb_host, s->d_rgb, bytes, cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return cuda_error(e, "cudaMemcpy (frame)");
+    if (rays_cast) {
+        unsigned long long c[2];
+        if ((e = cudaMemcpy(c, s->d_counters, sizeof(c), cudaMemcpyDeviceToHost)) != cudaSuccess)
+            return cuda_error(e, "cudaMemcpy (counters)");
+        rays_cast[0] = c[0];
+        rays_cast[1] = c[1];
+    }
+    return PRAY_OK;
+}
+
+pray_status pray_render_rt_counts(pray_scene *s, const pray_rt_params *p, uint64_t *out) {
+    if (!s || !out) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    pray_status st = check_params(p);
+    if (st != PRAY_OK) return st;
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    if ((st = ensure_frame(s, 3ull * p->width * p->height)) != PRAY_OK) return st;
+    if ((e = cudaMemsetAsync(s->d_counters, 0, 8 * sizeof(unsigned long long), 0)) != cudaSuccess)
+        return cuda_error(e, "cudaMemsetAsync");
+    RtLaunch L = make_launch(p);
+    L.rgb = s->d_rgb;
+    L.counters = s->d_counters;
+    L.count_fetches = 1;
+    if ((e = launch_render_rt(s->view(), L, 0)) != cudaSuccess) return cuda_error(e, "render_rt launch");
+    unsigned long long c[5];
+    if ((e = cudaMemcpy(c, s->d_counters, sizeof(c), cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return cuda_error(e, "cudaMemcpy (counters)");
+    for (int k = 0; k < 5; k++) out[k] = c[k];
+    return PRAY_OK;
+}
+
+pray_status pray_render_pt(pray_scene *s, const pray_pt_params *p, uint8_t *rgb, float *radiance,
+                           unsigned long long *counters, void *stream) {
+    if (!s || !rgb) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    pray_status st = check_pt_params(p);
+    if (st != PRAY_OK) return st;
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    PtLaunch L = make_pt_launch(p);
+    L.rgb = rgb;
+    L.radiance = radiance;
+    L.counters = counters;
+    e = launch_render_pt(s->view(), L, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_error(e, "render_pt launch");
+    return PRAY_OK;
+}
+
+pray_status pray_render_pt_host(pray_scene *s, const pray_pt_params *p, uint8_t *rgb_host, float *radiance_host,
+                                uint64_t *rays_cast) {
+    if (!s || !rgb_host) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    pray_status st = check_pt_params(p);
+    if (st != PRAY_OK) return st;
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    const uint64_t px = p->width * p->height;
+    if ((st = ensure_frame(s, 3 * px + (radiance_host ? 12 * px : 0))) != PRAY_OK) return st;
+    if ((e = cudaMemsetAsync(s->d_counters, 0, 2 * sizeof(unsigned long long), 0)) != cudaSuccess)
+        return cuda_error(e, "cudaMemsetAsync");
+    PtLaunch L = make_pt_launch(p);
+    L.rgb = s->d_rgb;
+    L.radiance = radiance_host ? reinterpret_cast<float *>(s->d_rgb + ((3 * px + 15) & ~15ull)) : nullptr;
+    L.counters = s->d_counters;
+    if ((e = launch_render_pt(s->view(), L, 0)) != cudaSuccess) return cuda_error(e, "render_pt launch");
+    if ((e = cudaMemcpy(rgb_host, s->d_rgb, 3 * px, cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return cuda_error(e, "cudaMemcpy (frame)");
+    if (radiance_host &&
+        (e = cudaMemcpy(radiance_host, L.radiance, 12 * px, cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return cuda_error(e, "cudaMemcpy (radiance)");
+    if (rays_cast) {
+        unsigned long long c[2];
+        if ((e = cudaMemcpy(c, s->d_counters, sizeof(c), cudaMemcpyDeviceToHost)) != cudaSuccess)
+            return cuda_error(e, "cudaMemcpy (counters)");
+        rays_cast[0] = c[0];
+        rays_cast[1] = c[1];
+    }
+    return PRAY_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,141 @@
+// Closest-hit tracing of caller-given rays and the fused ray-traced render
+// (primary ray, closest hit, Lambert shading with one occlusion ray per
+// light, quantisation). Traversal and intersection: traverse.cuh.
+#include <cfloat>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "device_layout.h"
+#include "trace_launch.h"
+#include "traverse.cuh"
+
+namespace pray_gpu {
+
+namespace {
+
+using namespace dev;
+
+__global__ void __launch_bounds__(128) k_trace_closest(DevScene s, const float *__restrict__ rays, uint64_t n,
+                                                       float eps, int32_t *__restrict__ ids,
+                                                       float *__restrict__ ts) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float *p = rays + 9 * i;
+    RayF r;
+    r.ox = p[0], r.oy = p[1], r.oz = p[2];
+    r.dx = p[3], r.dy = p[4], r.dz = p[5];
+    r.ix = p[6], r.iy = p[7], r.iz = p[8];
+    float t;
+    const int pos = traverse<false>(s, r, eps, 0.f, t);
+    ids[i] = pos >= 0 ? (int32_t)__float_as_uint(__ldg(&s.tris[pos].v0[3])) : -1;
+    ts[i] = t;
+}
+
+// Fused ray-tracing render: primary ray, closest hit, per-light Lambert with
+// an occlusion ray, clamp and quantise (evaluateRay, src/pray.cpp:17-55, and
+// the quantisation of src/pray.cpp:576-588).
+template <bool kCount>
+__global__ void __launch_bounds__(128) k_render_rt(DevScene s, RtLaunch L) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t px, py;
+    const bool active = pixel_of(i, L.cam.width, L.cam.height, px, py);
+    uint32_t shadows = 0;
+    bool shaded = false;
+    FetchCount fc;
+    if (active) {
+        const RayF r = primary_ray(L.cam, px, py);
+        float cr = L.bg[0], cg = L.bg[1], cb = L.bg[2];
+        float dist = FLT_MAX;
+        const int pos = (s.n_refs > 0) ? traverse<false, kCount>(s, r, L.eps, 0.f, dist, &fc) : -1;
+        int32_t id = -1;
+        shaded = pos >= 0;
+        if (pos >= 0) {
+            id = (int32_t)__float_as_uint(__ldg(&s.tris[pos].v0[3]));
+            const float4 nrm = __ldg(reinterpret_cast<const float4 *>(s.shade[id].n));
+            const float4 alb = __ldg(reinterpret_cast<const float4 *>(s.shade[id].c));
+            const float hx = r.ox + r.dx * dist, hy = r.oy + r.dy * dist, hz = r.oz + r.dz * dist;
+            cr = 0.f, cg = 0.f, cb = 0.f;
+            for (int l = 0; l < L.n_lights; l++) {
+                float lx = L.lights[l][0] - hx, ly = L.lights[l][1] - hy, lz = L.lights[l][2] - hz;
+                const float d2 = lx * lx + ly * ly + lz * lz;
+                if (d2 > 0) {
+                    const float inv = 1.0f / sqrtf(d2);
+                    lx *= inv, ly *= inv, lz *= inv;
+                }
+                const float lambert = lx * nrm.x + ly * nrm.y + lz * nrm.z;
+                if (lambert < 0.f) continue;
+                shadows++;
+                const RayF sr = make_ray(hx, hy, hz, lx, ly, lz);
+                float dummy;
+                if (traverse<true, kCount>(s, sr, L.eps, d2, dummy, &fc) >= 0) continue;
+                const float w = 1.0f / d2;
+                cr = cr + ((alb.x * L.lights[l][3]) * lambert) * w;
+                cg = cg + ((alb.y * L.lights[l][4]) * lambert) * w;
+                cb = cb + ((alb.z * L.lights[l][5]) * lambert) * w;
+                if (cr >= 1.f && cg >= 1.f && cb >= 1.f) break;
+            }
+            cr = smax(0.f, smin(1.f, cr));
+            cg = smax(0.f, smin(1.f, cg));
+            cb = smax(0.f, smin(1.f, cb));
+        }
+        uint8_t *o = L.rgb + 3ull * ((uint64_t)py * L.cam.width + px);
+        o[0] = (uint8_t)quantise(cr);
+        o[1] = (uint8_t)quantise(cg);
+        o[2] = (uint8_t)quantise(cb);
+        if (L.ids) {
+            const uint64_t pix = (uint64_t)py * L.cam.width + px;
+            L.ids[pix] = id;
+            L.ts[pix] = dist;
+        }
+    }
+    if (L.counters) {
+        // warp-aggregated ray counts: primary rays, occlusion rays
+        const uint32_t prim = __popc(__ballot_sync(0xFFFFFFFFu, active));
+        uint32_t sh = shadows;
+        for (int o = 16; o > 0; o >>= 1) sh += __shfl_xor_sync(0xFFFFFFFFu, sh, o);
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(L.counters + 0, (unsigned long long)prim);
+            atomicAdd(L.counters + 1, (unsigned long long)sh);
+        }
+        if (kCount) {
+            // node-pair fetches, triangle-reference fetches, shaded hits
+            unsigned long long pairs = fc.pairs, tris = fc.tris;
+            const uint32_t hits = __popc(__ballot_sync(0xFFFFFFFFu, active && shaded));
+            for (int o = 16; o > 0; o >>= 1) {
+                pairs += __shfl_xor_sync(0xFFFFFFFFu, pairs, o);
+                tris += __shfl_xor_sync(0xFFFFFFFFu, tris, o);
+            }
+            if ((threadIdx.x & 31) == 0) {
+                atomicAdd(L.counters + 2, pairs);
+                atomicAdd(L.counters + 3, tris);
+                atomicAdd(L.counters + 4, (unsigned long long)hits);
+            }
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_trace_closest(const DevScene &s, const float *rays, uint64_t n, float eps, int32_t *ids,
+                                 float *ts, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    const unsigned threads = 128;
+    const uint64_t blocks = (n + threads - 1) / threads;
+    k_trace_closest<<<(unsigned)blocks, threads, 0, stream>>>(s, rays, n, eps, ids, ts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_render_rt(const DevScene &s, const RtLaunch &L, cudaStream_t stream) {
+    const uint64_t tiles = (uint64_t)((L.cam.width + 7) / 8) * ((L.cam.height + 3) / 4);
+    const uint64_t threads = tiles * 32;
+    if (threads == 0) return cudaSuccess;
+    const unsigned bs = 128;
+    if (L.count_fetches)
+        k_render_rt<true><<<(unsigned)((threads + bs - 1) / bs), bs, 0, stream>>>(s, L);
+    else
+        k_render_rt<false><<<(unsigned)((threads + bs - 1) / bs), bs, 0, stream>>>(s, L);
+    return cudaGetLastError();
+}
+
+}  // namespace pray_gpu

@@ -1,0 +1,198 @@
+// Device-side ray traversal and intersection shared by the tracing kernels.
+//
+// Every translation unit that includes this file is built with --fmad=false
+// and IEEE division / square root, so each float operation rounds as in the
+// reference's scalar build compiled without FMA contraction.
+//
+// Traversal: one ray per thread, iterative, with a short per-thread stack.
+// Both children of a node are fetched together (one 64-byte pair) and tested
+// with the reference's infinite-line slab test (BoundingBox::intersect,
+// include/geometry.h:151-164); the nearer is entered first and the farther
+// pushed. Instead of the reference's visit-everything depth-first order
+// (KDTree::intersectRecursive, src/kd_tree.cpp:237-279), boxes that start
+// beyond the best hit found so far are skipped: the result is the
+// lexicographic minimum of (distance, depth-first reference position) over
+// the references the reference itself tests, which is exactly the triangle
+// it returns. The skip bounds keep a relative margin (kPruneRel) and an
+// absolute margin (DevScene::tol) so that rounding in a box's entry or exit
+// distance never drops a box holding the winning triangle.
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+
+#include "device_layout.h"
+#include "host/camera.h"
+
+namespace pray_gpu {
+namespace dev {
+
+constexpr float kPruneRel = 1.0f + 1.0f / 4096.0f;
+constexpr int kStack = 32;
+static_assert(kStack > kMaxTreeDepth, "stack must hold a full root-to-leaf path");
+
+struct RayF {
+    float ox, oy, oz;
+    float dx, dy, dz;
+    float ix, iy, iz;
+};
+
+__device__ __forceinline__ float smin(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float smax(float a, float b) { return (a < b) ? b : a; }
+
+// Ray ctor of include/geometry.h:82-87: normalise, then 1/direction.
+__device__ __forceinline__ RayF make_ray(float ox, float oy, float oz, float dx, float dy, float dz) {
+    RayF r;
+    r.ox = ox, r.oy = oy, r.oz = oz;
+    const float n2 = dx * dx + dy * dy + dz * dz;
+    if (n2 > 0) {
+        const float inv = 1.0f / sqrtf(n2);
+        dx *= inv, dy *= inv, dz *= inv;
+    }
+    r.dx = dx, r.dy = dy, r.dz = dz;
+    r.ix = 1.0f / dx, r.iy = 1.0f / dy, r.iz = 1.0f / dz;
+    return r;
+}
+
+// BoundingBox::intersect, include/geometry.h:151-164.
+__device__ __forceinline__ bool slab(const float4 &lo, const float4 &hi, const RayF &r, float &tn, float &tf) {
+    const float t1x = (lo.x - r.ox) * r.ix, t2x = (hi.x - r.ox) * r.ix;
+    const float t1y = (lo.y - r.oy) * r.iy, t2y = (hi.y - r.oy) * r.iy;
+    const float t1z = (lo.z - r.oz) * r.iz, t2z = (hi.z - r.oz) * r.iz;
+    tn = smax(smax(smin(t1x, t2x), smin(t1y, t2y)), smax(smin(t1z, t2z), -FLT_MAX));
+    tf = smin(smin(smax(t1x, t2x), smax(t1y, t2y)), smin(smax(t1z, t2z), FLT_MAX));
+    return tn <= tf;
+}
+
+// One-sided Moeller-Trumbore, include/geometry.h:242-262, with the det
+// threshold as a parameter (the reference's EPSILON is 1e-4).
+__device__ __forceinline__ bool intersect_tri(const float4 &v0, const float4 &e1, const float4 &e2, const RayF &r,
+                                              float eps, float &t) {
+    const float px = r.dy * e2.z - r.dz * e2.y;
+    const float py = r.dz * e2.x - r.dx * e2.z;
+    const float pz = r.dx * e2.y - r.dy * e2.x;
+    const float det = e1.x * px + e1.y * py + e1.z * pz;
+    if (det < eps) return false;
+    const float inv = 1.0f / det;
+    const float tx = r.ox - v0.x, ty = r.oy - v0.y, tz = r.oz - v0.z;
+    const float u = (tx * px + ty * py + tz * pz) * inv;
+    if (u < 0.f || u > 1.f) return false;
+    const float qx = ty * e1.z - tz * e1.y;
+    const float qy = tz * e1.x - tx * e1.z;
+    const float qz = tx * e1.y - ty * e1.x;
+    const float v = (r.dx * qx + r.dy * qy + r.dz * qz) * inv;
+    if (v < 0.f || u + v > 1.f) return false;
+    t = (e2.x * qx + e2.y * qy + e2.z * qz) * inv;
+    return true;
+}
+
+__device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
+
+// Closest hit (kAny = false): returns the reference position of the winning
+// triangle or -1, and its distance in t.
+// Any hit (kAny = true): returns >= 0 as soon as a triangle with t > 0 and
+// t * t < d2 is found (the occlusion test of src/pray.cpp:42).
+// Fetch counts of one traversal (only maintained when kCount is set).
+struct FetchCount {
+    uint32_t pairs = 0, tris = 0;
+};
+
+template <bool kAny, bool kCount = false>
+__device__ __forceinline__ int traverse(const DevScene &s, const RayF &r, float eps, float d2, float &best_t,
+                                        FetchCount *fc = nullptr) {
+    best_t = FLT_MAX;
+    int best = -1;
+    float tn, tf;
+    const float4 rlo = ldg4(s.nodes[0].lo), rhi = ldg4(s.nodes[0].hi);
+    if (!slab(rlo, rhi, r, tn, tf)) return -1;
+    uint32_t a = __float_as_uint(rlo.w), b = __float_as_uint(rhi.w);
+    float limit = kAny ? sqrtf(d2) * kPruneRel : FLT_MAX;
+    const float back = -s.tol;
+    uint32_t stk_a[kStack], stk_b[kStack];
+    float stk_t[kStack];
+    int sp = 0;
+    while (true) {
+        if (b & kLeafFlag) {
+            const uint32_t end = a + (b & ~kLeafFlag);
+            for (uint32_t i = a; i < end; i++) {
+                if (kCount) fc->tris++;
+                const GTri *T = s.tris + i;
+                const float4 v0 = ldg4(T->v0), e1 = ldg4(T->e1), e2 = ldg4(T->e2);
+                float t;
+                if (intersect_tri(v0, e1, e2, r, eps, t) && t > 0) {
+                    if (kAny) {
+                        if (d2 > t * t) return (int)i;
+                    } else if (t < best_t || (best >= 0 && t == best_t && (int)i < best)) {
+                        best_t = t;
+                        best = (int)i;
+                        limit = t * kPruneRel;
+                    }
+                }
+            }
+        } else {
+            if (kCount) fc->pairs++;
+            const GNode *c = s.nodes + a;
+            const float4 l0 = ldg4(c[0].lo), h0 = ldg4(c[0].hi), l1 = ldg4(c[1].lo), h1 = ldg4(c[1].hi);
+            float tn0, tf0, tn1, tf1;
+            const bool v0 = slab(l0, h0, r, tn0, tf0) && tn0 <= limit && tf0 >= back;
+            const bool v1 = slab(l1, h1, r, tn1, tf1) && tn1 <= limit && tf1 >= back;
+            if (v0 && v1) {
+                const bool first0 = tn0 <= tn1;
+                const float4 nl = first0 ? l0 : l1, nh = first0 ? h0 : h1;
+                const float4 fl = first0 ? l1 : l0, fh = first0 ? h1 : h0;
+                stk_a[sp] = __float_as_uint(fl.w);
+                stk_b[sp] = __float_as_uint(fh.w);
+                stk_t[sp] = first0 ? tn1 : tn0;
+                sp++;
+                a = __float_as_uint(nl.w);
+                b = __float_as_uint(nh.w);
+                continue;
+            }
+            if (v0 || v1) {
+                a = __float_as_uint(v0 ? l0.w : l1.w);
+                b = __float_as_uint(v0 ? h0.w : h1.w);
+                continue;
+            }
+        }
+        // pop the next box that can still hold a closer hit
+        bool found = false;
+        while (sp > 0) {
+            sp--;
+            if (stk_t[sp] <= limit) {
+                a = stk_a[sp];
+                b = stk_b[sp];
+                found = true;
+                break;
+            }
+        }
+        if (!found) break;
+    }
+    return kAny ? -1 : best;
+}
+
+// Primary ray of pixel (px, py), src/scene_preprocessor.cpp:124-134.
+__device__ __forceinline__ RayF primary_ray(const CameraConsts &c, uint32_t px, uint32_t py) {
+    const float x = (2 * (((float)px + 0.5f) * c.inv_w) - 1) * c.angle;
+    const float y = (1 - 2 * (((float)py + 0.5f) * c.inv_h)) * c.angle / c.aspect;
+    const float dx = x * c.m[0][0] + y * c.m[1][0] + c.m[2][0];
+    const float dy = x * c.m[0][1] + y * c.m[1][1] + c.m[2][1];
+    const float dz = x * c.m[0][2] + y * c.m[1][2] + c.m[2][2];
+    return make_ray(c.pos[0], c.pos[1], c.pos[2], dx, dy, dz);
+}
+
+// static_cast<uint8_t>(v * 255 + 0.5) on the reference's targets: truncate to
+// int, keep the low byte.
+__device__ __forceinline__ uint32_t quantise(float v) { return (uint32_t)(int32_t)(v * 255.f + 0.5f) & 0xFFu; }
+
+// Pixel index of thread i: warps cover 8x4 pixel tiles, tiles row-major.
+__device__ __forceinline__ bool pixel_of(uint64_t i, uint32_t w, uint32_t h, uint32_t &px, uint32_t &py) {
+    const uint32_t tiles_x = (w + 7) / 8;
+    const uint64_t tile = i >> 5;
+    const uint32_t lane = (uint32_t)i & 31u;
+    px = (uint32_t)(tile % tiles_x) * 8 + (lane & 7u);
+    py = (uint32_t)(tile / tiles_x) * 4 + (lane >> 3);
+    return px < w && py < h;
+}
+
+}  // namespace dev
+}  // namespace pray_gpu

@@ -233,3 +233,100 @@ def write_scene(path_json: str, mesh: Mesh, setup: RenderSetup, obj_name: Option
         doc["num_samples"] = setup.num_samples
     with open(path_json, "w") as fj:
         json.dump(doc, fj, indent=1)
+
+
+# --------------------------------------------------------------------------
+# Closed box room for path tracing: 2x2x2 room (x in [-1,1], y in [0,2],
+# z in [-1,1]) with inward-facing walls (white 0.75, red left wall, green right
+# wall), an emissive 0.5x0.5 ceiling quad just below the ceiling, and boxes
+# rotated about the vertical axis. Every face is a grid of quads split into
+# two triangles each; `grid` sets the quads per face edge (53 gives ~101k
+# triangles). The camera sits inside, in front of the front wall.
+
+WHITE = (0.75, 0.75, 0.75)
+RED = (0.63, 0.06, 0.05)
+GREEN = (0.14, 0.45, 0.09)
+
+
+def _quad_grid(origin, eu, ev, n: int) -> np.ndarray:
+    """Triangles of an n x n grid over the parallelogram origin + s*eu + t*ev,
+    wound so that (b-a) x (c-a) points along eu x ev."""
+    o, eu, ev = (np.asarray(x, np.float64) for x in (origin, eu, ev))
+    s = np.arange(n + 1) / n
+    P = o[None, None, :] + s[:, None, None] * eu[None, None, :] + s[None, :, None] * ev[None, None, :]
+    p00 = P[:-1, :-1].reshape(-1, 3)
+    p10 = P[1:, :-1].reshape(-1, 3)
+    p01 = P[:-1, 1:].reshape(-1, 3)
+    p11 = P[1:, 1:].reshape(-1, 3)
+    t1 = np.concatenate([p00, p10, p11], 1)
+    t2 = np.concatenate([p00, p11, p01], 1)
+    return np.stack([t1, t2], 1).reshape(-1, 9)
+
+
+def _box_faces(center, size, angle_deg, n: int) -> List[np.ndarray]:
+    """Outward-facing faces of a box rotated about +y, resting on y = 0."""
+    cx, cz = center
+    sx, sy, sz = size
+    a = np.radians(angle_deg)
+    R = np.array([[np.cos(a), 0, np.sin(a)], [0, 1, 0], [-np.sin(a), 0, np.cos(a)]])
+    hx, hz = sx / 2, sz / 2
+    local = [  # (origin, eu, ev) with eu x ev outward
+        ((-hx, 0, -hz), (0, sy, 0), (2 * hx, 0, 0)),  # -z face
+        ((-hx, 0, hz), (2 * hx, 0, 0), (0, sy, 0)),  # +z
+        ((-hx, 0, -hz), (0, 0, 2 * hz), (0, sy, 0)),  # -x
+        ((hx, 0, -hz), (0, sy, 0), (0, 0, 2 * hz)),  # +x
+        ((-hx, sy, -hz), (0, 0, 2 * hz), (2 * hx, 0, 0)),  # top
+        ((-hx, 0, -hz), (2 * hx, 0, 0), (0, 0, 2 * hz)),  # bottom
+    ]
+    out = []
+    for o, eu, ev in local:
+        o = R @ np.asarray(o, float) + np.array([cx, 0.0, cz])
+        out.append(_quad_grid(o, R @ np.asarray(eu, float), R @ np.asarray(ev, float), n))
+    return out
+
+
+def room(grid: int = 53, light_grid: int = 4, boxes=None, wall_albedo=WHITE, light_size: float = 0.5,
+         light_radiance=(17.0, 12.0, 4.0)) -> Mesh:
+    if boxes is None:
+        boxes = [((-0.35, -0.3), (0.55, 1.1, 0.55), 20.0, WHITE), ((0.4, 0.35), (0.55, 0.55, 0.55), -18.0, WHITE)]
+    parts, cols, emit = [], [], []
+
+    def add(tris, col, e=0):
+        parts.append(tris)
+        cols.append(np.tile(np.asarray(col, np.float64), (tris.shape[0], 1)))
+        emit.append(np.full(tris.shape[0], e, np.uint8))
+
+    # inward-facing walls (eu x ev points into the room)
+    add(_quad_grid((-1, 0, -1), (0, 0, 2), (2, 0, 0), grid), wall_albedo)  # floor, normal +y
+    add(_quad_grid((-1, 2, -1), (2, 0, 0), (0, 0, 2), grid), wall_albedo)  # ceiling, normal -y
+    add(_quad_grid((-1, 0, -1), (2, 0, 0), (0, 2, 0), grid), wall_albedo)  # back z=-1, normal +z
+    add(_quad_grid((-1, 0, 1), (0, 2, 0), (2, 0, 0), grid), wall_albedo)  # front z=+1, normal -z
+    add(_quad_grid((-1, 0, -1), (0, 2, 0), (0, 0, 2), grid), RED)  # left x=-1, normal +x
+    add(_quad_grid((1, 0, -1), (0, 0, 2), (0, 2, 0), grid), GREEN)  # right x=+1, normal -x
+    h = light_size / 2
+    add(_quad_grid((-h, 1.999, -h), (2 * h, 0, 0), (0, 0, 2 * h), light_grid), light_radiance, 1)  # normal -y
+    for center, size, ang, col in boxes:
+        for f in _box_faces(center, size, ang, grid):
+            add(f, col)
+    verts = np.concatenate(parts).astype(np.float32)
+    return Mesh(verts, np.concatenate(cols).astype(np.float32), np.concatenate(emit))
+
+
+def room_setup(width: int = 1024, height: int = 1024, spp: int = 64, max_depth: int = 8) -> RenderSetup:
+    return RenderSetup(width=width, height=height, fov=60, cam_pos=(0.0, 1.0, 0.98), cam_look=(0.0, 0.0, -1.0),
+                       lights=[], tree="sah", leaf_size=32, max_depth=20, sah_ct=1.0, sah_ci=1.5, det_eps=0.0,
+                       method="path_tracing", max_depth_pt=max_depth, num_samples=spp)
+
+
+def random_room(seed: int, grid: int = 16) -> Mesh:
+    """Procedural room: 1-6 random boxes, wall albedo U[0.1,0.9]^3, light size
+    U[0.3,0.8]."""
+    rng = np.random.default_rng(seed)
+    nb = int(rng.integers(1, 7))
+    boxes = []
+    for _ in range(nb):
+        c = tuple(rng.uniform(-0.6, 0.6, 2))
+        s = (float(rng.uniform(0.2, 0.6)), float(rng.uniform(0.2, 1.2)), float(rng.uniform(0.2, 0.6)))
+        boxes.append((c, s, float(rng.uniform(-45, 45)), tuple(rng.uniform(0.1, 0.9, 3))))
+    return room(grid=grid, boxes=boxes, wall_albedo=tuple(rng.uniform(0.1, 0.9, 3)),
+                light_size=float(rng.uniform(0.3, 0.8)))

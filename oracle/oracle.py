@@ -69,6 +69,12 @@ def lib():
         L.orc_render_rt.restype = _u64
         L.orc_render_rt.argtypes = [_vp, _u64, _u64, _u64, _f32p, _f32p, _f32p, ctypes.c_int, _f32p,
                                     ctypes.c_float, _u64, _u64, _u8p, ctypes.c_int]
+        L.orc_sincos_turns.argtypes = [_f32p, _u64, _f32p, _f32p]
+        L.orc_sample_hemisphere.argtypes = [_f32p, _f32p, _u64, _f32p]
+        L.orc_render_pt.restype = _u64
+        L.orc_render_pt.argtypes = [_vp, _u64, _u64, _u64, _f32p, _f32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
+                                    _u64, ctypes.c_float, ctypes.c_int, ctypes.c_uint32, _u64, _u64, _u8p,
+                                    _vp, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -90,6 +96,22 @@ def primary_rays(width, height, fov, cam_pos, cam_look) -> np.ndarray:
 def camera(width, height, fov, cam_pos, cam_look) -> np.ndarray:
     out = np.empty(13, np.float32)
     lib().orc_camera(width, height, fov, _f3(cam_pos), _f3(cam_look), out)
+    return out
+
+
+def sincos_turns(u: np.ndarray):
+    u = np.ascontiguousarray(u, np.float32)
+    s = np.empty_like(u)
+    c = np.empty_like(u)
+    lib().orc_sincos_turns(u, u.size, s, c)
+    return s, c
+
+
+def sample_hemisphere(normals: np.ndarray, u: np.ndarray) -> np.ndarray:
+    normals = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+    u = np.ascontiguousarray(u, np.float32).reshape(-1, 2)
+    out = np.empty_like(normals)
+    lib().orc_sample_hemisphere(normals, u, normals.shape[0], out)
     return out
 
 
@@ -155,6 +177,18 @@ class OracleScene(_TreeDumpMixin):
                                   lights.shape[0], _f3(setup.background), setup.det_eps, r0, r1, out,
                                   threads or default_threads())
         return out, int(nsh)
+
+    def render_pt(self, setup, spp: int, max_depth: int, seed: int = 0, mode: int = 0, rr_depth: int = 3,
+                  rows: Optional[Sequence[int]] = None, threads: Optional[int] = None):
+        """Returns (rgb uint8 (rows, width, 3), mean radiance float32, segments)."""
+        r0, r1 = (0, setup.height) if rows is None else rows
+        out = np.empty((r1 - r0, setup.width, 3), np.uint8)
+        rad = np.empty((r1 - r0, setup.width, 3), np.float32)
+        segs = lib().orc_render_pt(self._h, setup.width, setup.height, setup.fov, _f3(setup.cam_pos),
+                                   _f3(setup.cam_look), _f3(setup.background), max_depth, spp, seed,
+                                   setup.det_eps, mode, rr_depth, r0, r1, out, rad.ctypes.data,
+                                   threads or default_threads())
+        return out, rad, int(segs)
 
 
 # --------------------------------------------------------------------------

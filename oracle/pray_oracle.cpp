@@ -19,6 +19,8 @@
 #include <memory>
 #include <vector>
 
+#include "../include/nostrum_pray_sampling.h"
+
 
 namespace {
 
@@ -508,9 +510,190 @@ inline uint8_t quantise(float c) {
     return (uint8_t)(uint32_t)(int32_t)v;
 }
 
+// ---- path tracing -----------------------------------------------------------
+// Kajiya mode restates evaluatePathRecursive / evaluatePath
+// (src/pray.cpp:342-378) with the PCG32 streams and hemisphere sampling of
+// include/nostrum_pray_sampling.h in place of the reference's clock-seeded
+// mt19937_64. NEE mode is this project's next-event-estimation variant (no
+// reference counterpart); the CUDA kernel must match this code's float
+// operation order.
+
+struct Emitters {
+    std::vector<int64_t> ids;
+    std::vector<float> cdf;
+    float area = 0.f;
+};
+
+Emitters collect_emitters(const Scene &s) {
+    Emitters e;
+    double acc = 0.0;
+    for (size_t i = 0; i < s.tris.size(); i++) {
+        const Tri &t = s.tris[i];
+        if (!t.emit) continue;
+        const V3 c = cross(t.ab, t.ac);
+        const double a = 0.5 * std::sqrt((double)c.x * c.x + (double)c.y * c.y + (double)c.z * c.z);
+        if (!(a > 0.0)) continue;
+        acc += a;
+        e.ids.push_back((int64_t)i);
+        e.cdf.push_back((float)acc);
+    }
+    e.area = e.cdf.empty() ? 0.f : e.cdf.back();
+    return e;
+}
+
+V3 path_kajiya(const Scene &s, Ray r, V3 bg, uint32_t max_depth, float eps, pray_pcg32 &g, uint64_t &segs) {
+    std::vector<V3> albedo;
+    V3 L;
+    while (true) {
+        int64_t id;
+        float t;
+        segs++;
+        if (!closest(s, r, eps, id, t)) {
+            L = bg;
+            break;
+        }
+        const Tri &tri = s.tris[id];
+        if (tri.emit) {
+            L = tri.color;
+            break;
+        }
+        if (albedo.size() >= max_depth) {
+            L = {0.f, 0.f, 0.f};
+            break;
+        }
+        albedo.push_back(tri.color);
+        V3 hit = add(r.o, scale(r.d, t));
+        const float u1 = pray_uniform(&g), u2 = pray_uniform(&g);
+        const float n[3] = {tri.normal.x, tri.normal.y, tri.normal.z};
+        float d[3];
+        pray_sample_hemisphere(n, u1, u2, d);
+        r = make_ray(hit, {d[0], d[1], d[2]});
+    }
+    for (size_t k = albedo.size(); k-- > 0;) L = mul(L, albedo[k]);
+    return L;
+}
+
+V3 path_nee(const Scene &s, const Emitters &em, Ray r, V3 bg, uint32_t max_depth, uint32_t rr_depth, float eps,
+            pray_pcg32 &g, uint64_t &segs) {
+    V3 T{1.f, 1.f, 1.f}, L{0.f, 0.f, 0.f};
+    const float inv_pi = 0.318309886183790671538f;
+    for (uint32_t depth = 0;; depth++) {
+        int64_t id;
+        float t;
+        segs++;
+        if (!closest(s, r, eps, id, t)) {
+            L = add(L, mul(T, bg));
+            break;
+        }
+        const Tri &tri = s.tris[id];
+        if (tri.emit) {
+            if (depth == 0) L = add(L, mul(T, tri.color));
+            break;
+        }
+        if (depth >= max_depth) break;
+        const V3 hit = add(r.o, scale(r.d, t));
+        if (!em.ids.empty()) {
+            const float ue = pray_uniform(&g), ua = pray_uniform(&g), ub = pray_uniform(&g);
+            const float target = ue * em.area;
+            size_t lo = 0, hi = em.ids.size() - 1;
+            while (lo < hi) {
+                const size_t mid = (lo + hi) >> 1;
+                if (em.cdf[mid] > target) hi = mid;
+                else lo = mid + 1;
+            }
+            const Tri &E = s.tris[em.ids[lo]];
+            const float su = std::sqrt(ua);
+            const float b1 = su * (1.f - ub), b2 = su * ub;
+            const V3 y{E.a.x + E.ab.x * b1 + E.ac.x * b2, E.a.y + E.ab.y * b1 + E.ac.y * b2,
+                       E.a.z + E.ab.z * b1 + E.ac.z * b2};
+            V3 w = sub(y, hit);
+            const float d2 = w.x * w.x + w.y * w.y + w.z * w.z;
+            if (d2 > 0.f) {
+                const float inv = 1.0f / std::sqrt(d2);
+                w = {w.x * inv, w.y * inv, w.z * inv};
+                const float cx = dot(tri.normal, w);
+                const float cy = -dot(E.normal, w);
+                if (cx > 0.f && cy > 0.f) {
+                    segs++;
+                    int64_t sid;
+                    float st;
+                    const bool blocked = closest(s, make_ray(hit, w), eps, sid, st) && d2 * 0.999f > st * st;
+                    if (!blocked) {
+                        const float gterm = ((cx * cy) * em.area) * inv_pi / d2;
+                        L = {L.x + ((T.x * tri.color.x) * E.color.x) * gterm, L.y + ((T.y * tri.color.y) * E.color.y) * gterm,
+                             L.z + ((T.z * tri.color.z) * E.color.z) * gterm};
+                    }
+                }
+            }
+        }
+        const float u1 = pray_uniform(&g), u2 = pray_uniform(&g);
+        const float n[3] = {tri.normal.x, tri.normal.y, tri.normal.z};
+        float d[3];
+        pray_sample_hemisphere(n, u1, u2, d);
+        r = make_ray(hit, {d[0], d[1], d[2]});
+        T = mul(T, tri.color);
+        if (depth >= rr_depth) {
+            const float q = smin(smax(smax(T.x, T.y), T.z), 0.95f);
+            if (!(pray_uniform(&g) < q)) break;
+            T = {T.x / q, T.y / q, T.z / q};
+        }
+    }
+    return L;
+}
+
 }  // namespace
 
 extern "C" {
+
+// cos/sin(2 pi u) of the shared sampling header, for accuracy tests.
+void orc_sincos_turns(const float *u, uint64_t n, float *s_out, float *c_out) {
+    for (uint64_t i = 0; i < n; i++) pray_sincos_turns(u[i], s_out + i, c_out + i);
+}
+
+void orc_sample_hemisphere(const float *normals, const float *u, uint64_t n, float *dirs) {
+    for (uint64_t i = 0; i < n; i++) pray_sample_hemisphere(normals + 3 * i, u[2 * i], u[2 * i + 1], dirs + 3 * i);
+}
+
+// Path-traced rows [row0, row1): out_rgb width*(row1-row0)*3 bytes, out_rad
+// (may be NULL) the mean radiance per pixel. Returns the ray segments cast.
+uint64_t orc_render_pt(void *h, uint64_t w, uint64_t hh, uint64_t fov, const float *pos, const float *look,
+                       const float *bg, uint32_t max_depth, uint32_t spp, uint64_t seed, float eps, int mode,
+                       uint32_t rr_depth, uint64_t row0, uint64_t row1, uint8_t *out_rgb, float *out_rad,
+                       int threads) {
+    auto &s = *static_cast<Scene *>(h);
+    Camera c = make_camera(w, hh, fov, {pos[0], pos[1], pos[2]}, {look[0], look[1], look[2]});
+    const Emitters em = collect_emitters(s);
+    const V3 b{bg[0], bg[1], bg[2]};
+    uint64_t segs = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : segs) num_threads(threads > 0 ? threads : 1)
+    for (uint64_t py = row0; py < row1; py++) {
+        for (uint64_t px = 0; px < w; px++) {
+            const uint64_t pixel = py * w + px;
+            const Ray prim = primary(c, px, py);
+            V3 sum{0.f, 0.f, 0.f};
+            for (uint32_t k = 0; k < spp; k++) {
+                pray_pcg32 g = pray_pcg32_stream(seed, pixel, k);
+                const V3 L = mode == 0 ? path_kajiya(s, prim, b, max_depth, eps, g, segs)
+                                       : path_nee(s, em, prim, b, max_depth, rr_depth, eps, g, segs);
+                sum = add(sum, L);
+            }
+            const float ns = (float)spp;
+            const V3 mean{sum.x / ns, sum.y / ns, sum.z / ns};
+            const uint64_t o = (py - row0) * w + px;
+            if (out_rad) {
+                out_rad[3 * o] = mean.x;
+                out_rad[3 * o + 1] = mean.y;
+                out_rad[3 * o + 2] = mean.z;
+            }
+            auto cl = [](float v) { return smax(0.f, smin(1.f, v)); };
+            out_rgb[3 * o] = quantise(cl(mean.x));
+            out_rgb[3 * o + 1] = quantise(cl(mean.y));
+            out_rgb[3 * o + 2] = quantise(cl(mean.z));
+        }
+    }
+    return segs;
+}
+
 
 void *orc_scene_new(const float *verts, const float *colors, const uint8_t *emit, uint64_t n) {
     auto *s = new Scene();

@@ -1,0 +1,177 @@
+"""Parity of the CUDA ray-tracing path with the oracle (GPU).
+
+Every comparison is bit-exact: hit triangle ids, hit distances (as bit
+patterns) and image bytes. The oracle itself is pinned against the reference
+(test_oracle_golden.py), and the full-size cases are also checked against the
+digests the reference produced (tests/golden/golden_hashes.json)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from golden_util import sha
+from nostrum_pray_gb300 import native, scenes
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    native.lib()
+    torch.cuda.set_device(0)
+
+
+def render(sc, setup):
+    h, w = setup.height, setup.width
+    rgb = torch.empty((h, w, 3), dtype=torch.uint8, device="cuda")
+    ids = torch.empty((h, w), dtype=torch.int32, device="cuda")
+    ts = torch.empty((h, w), dtype=torch.float32, device="cuda")
+    cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+    sc.render_rt(setup, rgb, ids, ts, cnt)
+    torch.cuda.synchronize()
+    return rgb.cpu().numpy(), ids.cpu().numpy().reshape(-1), ts.cpu().numpy().reshape(-1), cnt.cpu().numpy()
+
+
+def trace(sc, rays, eps):
+    r = torch.from_numpy(np.ascontiguousarray(rays, np.float32)).cuda()
+    n = rays.shape[0]
+    ids = torch.empty(n, dtype=torch.int32, device="cuda")
+    ts = torch.empty(n, dtype=torch.float32, device="cuda")
+    sc.trace_closest(r, eps, ids, ts)
+    torch.cuda.synchronize()
+    return ids.cpu().numpy(), ts.cpu().numpy()
+
+
+def check_frame(oracle, mesh, setup):
+    sc = native.Scene.from_setup(mesh, setup)
+    img, ids, ts, cnt = render(sc, setup)
+    orc = oracle.OracleScene.from_setup(mesh, setup)
+    want_img, want_sh = orc.render_rt(setup)
+    rays = oracle.primary_rays(setup.width, setup.height, setup.fov, setup.cam_pos, setup.cam_look)
+    want_ids, want_t = orc.trace(rays, setup.det_eps)
+    mism = int((ids != want_ids.astype(np.int32)).sum())
+    assert mism == 0, f"{mism} hit ids differ"
+    np.testing.assert_array_equal(ts.view(np.uint32), want_t.view(np.uint32))
+    np.testing.assert_array_equal(img, want_img)
+    assert int(cnt[0]) == setup.width * setup.height
+    assert int(cnt[1]) == want_sh
+    # host-memory entry point gives the same frame
+    himg, rays_cast = sc.render_rt_host(setup)
+    np.testing.assert_array_equal(himg, want_img)
+    assert int(rays_cast[1]) == want_sh
+    return img, ids, ts
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_soup_frame(oracle, seed):
+    check_frame(oracle, scenes.soup(10_000, seed), scenes.soup_setup())
+
+
+def test_soup_sah_default_constants(oracle):
+    st = scenes.soup_setup(320, 240)
+    st.tree, st.leaf_size, st.max_depth = "sah", 32, 20
+    check_frame(oracle, scenes.soup(10_000, 4), st)
+
+
+@pytest.mark.parametrize("eps", [0.0, 1e-4])
+def test_icosphere_level5(oracle, golden, eps):
+    hashes, small = golden
+    st = scenes.icosphere_setup(480, 270, det_eps=eps)
+    img, ids, ts = check_frame(oracle, scenes.icosphere(5), st)
+    key = f"ico5_eps{eps:g}"
+    assert sha(img) == hashes[key]["image"]  # the reference's own frame
+    assert sha(ids) == hashes[key]["ids"] and sha(ts) == hashes[key]["t"]
+
+
+@pytest.mark.parametrize("name", ["cube", "head_fov30", "plant"])
+def test_examples(oracle, golden, name):
+    hashes, small = golden
+    info = small[f"ex_{name}_info"]
+    m = scenes.Mesh(small[f"ex_{name}_verts"], small[f"ex_{name}_colors"], small[f"ex_{name}_emit"])
+    st = scenes.RenderSetup(width=160, height=120, fov=int(info[2]), cam_pos=tuple(info[6:9]),
+                            cam_look=tuple(info[9:12]), lights=[tuple(l) for l in small[f"ex_{name}_lights"]],
+                            background=tuple(info[12:15]), tree="median")
+    img, _, _ = check_frame(oracle, m, st)
+    np.testing.assert_array_equal(img, small[f"ex_{name}_image160"])
+
+
+def test_random_rays_inside_scene(oracle):
+    """Rays from inside the soup in random directions, including exact axis
+    directions and zero components (infinite inverse directions)."""
+    m = scenes.soup(10_000, 5)
+    st = scenes.soup_setup()
+    sc = native.Scene.from_setup(m, st)
+    orc = oracle.OracleScene.from_setup(m, st)
+    rng = np.random.default_rng(0)
+    n = 200_000
+    o = rng.uniform(-0.2, 1.2, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d[: n // 10, 1:] = 0.0          # +-x axis rays
+    d[n // 10: n // 5, 0] = 0.0      # rays in the yz plane
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    with np.errstate(divide="ignore"):
+        inv = (1.0 / d).astype(np.float32)
+    rays = np.concatenate([o, d, inv], 1)
+    for eps in (1e-4, 0.0):
+        ids, ts = trace(sc, rays, eps)
+        wid, wt = orc.trace(rays, eps)
+        assert int((ids != wid.astype(np.int32)).sum()) == 0
+        np.testing.assert_array_equal(ts.view(np.uint32), wt.view(np.uint32))
+
+
+def test_ties_duplicated_triangles(oracle):
+    """Coincident copies of each triangle: equal distances, so the first in
+    the reference's depth-first order must win."""
+    base = scenes.soup(3_000, 9)
+    m = scenes.Mesh(np.concatenate([base.verts, base.verts[::-1]]), np.concatenate([base.colors, base.colors]),
+                    np.zeros(6_000, np.uint8))
+    for tree in ("median", "sah"):
+        st = scenes.soup_setup(256, 256)
+        st.tree = tree
+        check_frame(oracle, m, st)
+
+
+def test_empty_and_tiny_scenes(oracle):
+    st = scenes.soup_setup(33, 17)  # ragged size: partial 8x4 tiles
+    st.background = (0.25, 0.5, 1.0)
+    empty = scenes.Mesh(np.zeros((0, 9), np.float32), np.zeros((0, 3), np.float32), np.zeros(0, np.uint8))
+    sc = native.Scene.from_setup(empty, st)
+    img, _ = sc.render_rt_host(st)
+    want = np.array([int(np.float32(c) * np.float32(255) + np.float32(0.5)) for c in st.background], np.uint8)
+    assert (img == want).all()
+    one = scenes.Mesh(np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32) + np.float32(0.5) * 0,
+                      np.array([[0.5, 0.6, 0.7]], np.float32), np.zeros(1, np.uint8))
+    st2 = scenes.RenderSetup(width=64, height=48, fov=60, cam_pos=(0.2, 0.2, -2.0), cam_look=(0, 0, 1),
+                             lights=[(0.2, 0.2, -1.0, 1, 1, 1)])
+    check_frame(oracle, one, st2)
+
+
+def test_invalid_arguments_raise():
+    st = scenes.soup_setup(16, 16)
+    m = scenes.soup(100, 0)
+    with pytest.raises(native.PrayError):
+        native.Scene(m, native.tree_options(st, max_depth=31))
+    sc = native.Scene.from_setup(m, st)
+    bad = scenes.soup_setup(0, 16)
+    with pytest.raises(native.PrayError):
+        sc.render_rt_host(bad)
+
+
+@pytest.mark.slow
+def test_icosphere_level8_full(oracle, golden):
+    """The 1.31M-triangle displaced sphere at 1920x1080 with the SAH tree:
+    GPU frame == oracle frame == the reference's frame (digests)."""
+    hashes, _ = golden
+    m = scenes.icosphere(8)
+    for eps in (0.0, 1e-4):
+        st = scenes.icosphere_setup(det_eps=eps)
+        img, ids, ts = check_frame(oracle, m, st)
+        key = f"ico8_eps{eps:g}"
+        assert sha(img) == hashes[key]["image"]
+        assert sha(ids) == hashes[key]["ids"] and sha(ts) == hashes[key]["t"]
