@@ -24,6 +24,8 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CU_SOURCES = ["trace.cu", "pt.cu"]
 CPP_SOURCES = ["capi.cpp", "host/kdtree.cpp", "host/camera.cpp"]
 CLI_SOURCES = ["cli/pray_main.cpp", "cli/scene_io.cpp"]
+DUMP_SOURCES = ["cli/scene_dump.cpp"]
+DUMP = os.path.join(BUILD, "pray_scene_dump")
 
 NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xptxas", "-v"]
@@ -67,7 +69,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         o = _obj(s)
         if force or _stale(o, [src] + hdrs):
             jobs.append([nvcc] + NVCC_FLAGS + ["-c", src, "-o", o])
-    for s in CPP_SOURCES + CLI_SOURCES:
+    for s in CPP_SOURCES + CLI_SOURCES + DUMP_SOURCES:
         src = os.path.join(CSRC, s)
         o = _obj(s)
         if force or _stale(o, [src] + hdrs):
@@ -86,6 +88,10 @@ def build(verbose: bool = False, force: bool = False) -> str:
     if force or _stale(CLI, cli_objs + [LIB]):
         _run(["g++", "-o", CLI + ".tmp"] + cli_objs + [LIB, "-Wl,-rpath,$ORIGIN", "-pthread"], log)
         os.replace(CLI + ".tmp", CLI)
+    dump_objs = [_obj("cli/scene_dump.cpp"), _obj("cli/scene_io.cpp")]
+    if force or _stale(DUMP, dump_objs):
+        _run(["g++", "-o", DUMP + ".tmp"] + dump_objs, log)
+        os.replace(DUMP + ".tmp", DUMP)
     if verbose:
         sys.stdout.write("\n".join(log))
     with open(os.path.join(BUILD, "build.log"), "a") as f:

@@ -145,6 +145,25 @@ def main():
                                 "n": n, "lights": nl}
         print("example", name, n, nl, flush=True)
 
+    # -- hand-written OBJ/MTL cases (tests/golden/obj_cases) through the
+    #    reference's loader: polygons, negative indices, CRLF, exponent and
+    #    bare-fraction numbers, usemtl / o / g flushing
+    for name in ("poly", "shapes"):
+        L = O.ref_lib("default")
+        hnd = L.ref_scene_from_json(os.path.join(HERE, "obj_cases", name + ".json").encode())
+        info = np.zeros(17, np.float64)
+        L.ref_scene_info(hnd, info)
+        n, nl = int(info[16]), int(info[15])
+        verts = np.empty((n, 9), np.float32)
+        cols = np.empty((n, 3), np.float32)
+        emit = np.empty(n, np.uint8)
+        lights = np.empty((max(nl, 1), 6), np.float32)
+        L.ref_scene_get(hnd, verts, cols, emit, lights)
+        L.ref_scene_free(hnd)
+        for k, v in (("info", info), ("verts", verts), ("colors", cols), ("emit", emit), ("lights", lights[:nl])):
+            small[f"objcase_{name}_{k}"] = v
+        print("obj case", name, n, nl)
+
     # -- loader round trip: scenes.write_scene output read by the reference --
     with tempfile.TemporaryDirectory() as td:
         m = scenes.soup(500, 7)
