@@ -41,6 +41,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["icosphere", "soup"], default="icosphere")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--leaf-refine", type=int, default=4,
+                    help="device layout: sub-hierarchy inside reference leaves larger than this (0 = off)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     return ap.parse_args()
 
@@ -219,7 +221,7 @@ def run_ours(args):
         build.build()
     mesh, setup, cfg = workload(args.workload)
     t0 = time.perf_counter()
-    sc = native.Scene.from_setup(mesh, setup, device=dev)
+    sc = native.Scene.from_setup(mesh, setup, device=dev, leaf_refine=args.leaf_refine)
     build_s = time.perf_counter() - t0
     h, w = setup.height, setup.width
     rgb = torch.empty((h, w, 3), dtype=torch.uint8, device="cuda")
@@ -287,7 +289,8 @@ def run_ours(args):
         cpu = {"value": round(v, 4), "unit": "Mrays/s", "cores": cores, "kind": "port", "sample": sample}
     cfg = dict(cfg)
     cfg.update({"parallelism": f"replicas x{world}", "l2": "flushed between steps (256 MB write)",
-                "tree_build_s": round(build_s, 2), "rays_per_frame": rays_per_frame})
+                "tree_build_s": round(build_s, 2), "rays_per_frame": rays_per_frame,
+                "leaf_refine": args.leaf_refine})
     line = {"metric": "Mrays/s", "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(kernel_ms_max / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",

@@ -52,6 +52,8 @@ typedef struct {
     float sah_traversal_cost;      /* traversalCost (5) */
     float sah_intersection_cost;   /* triangleIntersectionCost (1.5) */
     int32_t build_threads;         /* host threads for the build, 0 = all */
+    int32_t leaf_refine;           /* device layout only: leaves with more references than this get a
+                                      conservative sub-hierarchy (4; 0 = off). Results are unchanged. */
 } pray_tree_options;
 
 /* Ray-tracing frame parameters: the scene JSON's camera, lights and
@@ -113,6 +115,11 @@ pray_status pray_host_tree_dump(const pray_host_tree *t, float *boxes, float *sp
                                 int64_t *refs);
 /* Per triangle: box min[3], box max[3], midpoint[3], b-a[3], c-a[3], normal[3]. */
 pray_status pray_host_tree_precompute(const pray_host_tree *t, float *out18);
+
+/* The device layout this tree would be uploaded as (no device work):
+ * out[4] = node records, triangle references, refined leaves, nodes added by
+ * the refinement. Fails if the layout would not pass the upload checks. */
+pray_status pray_host_tree_device_layout(const pray_host_tree *t, int32_t leaf_refine, uint64_t *out);
 
 /* Camera constants the kernels use: inverse view matrix rows 0-2 (columns
  * 0-2), 1/width, 1/height, aspect, tan(fov/2) — 13 floats

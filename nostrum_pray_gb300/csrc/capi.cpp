@@ -16,6 +16,7 @@
 #include "capi_internal.h"
 #include "device_layout.h"
 #include "host/camera.h"
+#include "host/flatten.h"
 #include "host/kdtree.h"
 #include "trace_launch.h"
 
@@ -52,6 +53,10 @@ bool valid_options(const pray_tree_options *opt, std::string &why) {
         why = "max_depth must be in [0, 30]";
         return false;
     }
+    if (opt->leaf_refine < 0) {
+        why = "leaf_refine must be >= 0";
+        return false;
+    }
     if (!(opt->sah_traversal_cost >= 0.f) || !(opt->sah_intersection_cost > 0.f)) {
         why = "SAH costs must be finite, traversal >= 0 and intersection > 0";
         return false;
@@ -68,32 +73,6 @@ TreeOptions to_options(const pray_tree_options *opt) {
     o.sah_ci = opt->sah_intersection_cost;
     o.threads = opt->build_threads;
     return o;
-}
-
-// Flattening into sibling-pair nodes; refs keep their DFS order.
-void flatten_device(const BuiltTree &t, std::vector<GNode> &out) {
-    out.assign(2, GNode{});
-    struct Rec {
-        static void put(const BuiltTree &t, int32_t p, uint32_t slot, std::vector<GNode> &out) {
-            const FlatNode &n = t.nodes[p];
-            GNode g;
-            for (int k = 0; k < 3; k++) g.lo[k] = n.box.lo[k], g.hi[k] = n.box.hi[k];
-            if (n.left < 0) {
-                g.a = n.first;
-                g.b = kLeafFlag | n.count;
-                out[slot] = g;
-                return;
-            }
-            const uint32_t pair = (uint32_t)out.size();
-            out.resize(out.size() + 2);
-            g.a = pair;
-            g.b = 0;
-            out[slot] = g;
-            put(t, n.left, pair, out);
-            put(t, n.right, pair + 1, out);
-        }
-    };
-    Rec::put(t, 0, 0, out);
 }
 
 }  // namespace pray_gpu
@@ -115,6 +94,7 @@ struct pray_scene {
     uint32_t n_emit = 0;
     float emit_area = 0.f;
     uint32_t n_gnodes = 0;
+    uint64_t refined_leaves = 0;
     float tol = 0.f;
     uint64_t device_bytes = 0;
     // frame buffers of the host-memory entry points, grown on demand
@@ -264,6 +244,7 @@ void pray_tree_options_default(pray_tree_options *opt) {
     opt->sah_traversal_cost = 5.f;
     opt->sah_intersection_cost = 1.5f;
     opt->build_threads = 0;
+    opt->leaf_refine = 4;
 }
 
 pray_status pray_host_tree_build(const float *verts, uint64_t n, const pray_tree_options *opt,
@@ -307,6 +288,22 @@ pray_status pray_host_tree_precompute(const pray_host_tree *t, float *out) {
     return PRAY_OK;
 }
 
+pray_status pray_host_tree_device_layout(const pray_host_tree *t, int32_t leaf_refine, uint64_t *out) {
+    if (!t || !out) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (leaf_refine < 0) return set_error(PRAY_ERR_INVALID_ARGUMENT, "leaf_refine must be >= 0");
+    PRAY_TRY({
+        DeviceImage img;
+        flatten_for_device(t->tree, t->tris, leaf_refine, img);
+        std::string bad;
+        if (!validate_device_image(img, bad)) return set_error(PRAY_ERR_UNSUPPORTED, "device layout: " + bad);
+        out[0] = img.nodes.size();
+        out[1] = img.tris.size();
+        out[2] = img.refined_leaves;
+        out[3] = img.sub_nodes;
+        return PRAY_OK;
+    })
+}
+
 pray_status pray_camera(uint64_t width, uint64_t height, uint64_t fov, const float *pos, const float *look,
                         float *out) {
     if (!pos || !look || !out) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
@@ -343,19 +340,13 @@ pray_status pray_scene_create(const float *verts, const float *colors, const uin
         s->tree = build_tree(pre, to_options(opt));
         if (s->tree.refs.size() >= (1ull << 31))
             return set_error(PRAY_ERR_UNSUPPORTED, "more than 2^31-1 leaf references");
-        flatten_device(s->tree, gnodes);
-        gtris.resize(s->tree.refs.size());
-        for (size_t i = 0; i < s->tree.refs.size(); i++) {
-            const uint32_t id = s->tree.refs[i];
-            const TriPre &p = pre[id];
-            GTri &g = gtris[i];
-            uint32_t idbits = id;
-            float idf;
-            std::memcpy(&idf, &idbits, 4);
-            g.v0[0] = p.a[0], g.v0[1] = p.a[1], g.v0[2] = p.a[2], g.v0[3] = idf;
-            g.e1[0] = p.ab[0], g.e1[1] = p.ab[1], g.e1[2] = p.ab[2], g.e1[3] = 0.f;
-            g.e2[0] = p.ac[0], g.e2[1] = p.ac[1], g.e2[2] = p.ac[2], g.e2[3] = 0.f;
-        }
+        DeviceImage img;
+        flatten_for_device(s->tree, pre, opt->leaf_refine, img);
+        std::string bad;
+        if (!validate_device_image(img, bad)) return set_error(PRAY_ERR_UNSUPPORTED, "device layout: " + bad);
+        gnodes.swap(img.nodes);
+        gtris.swap(img.tris);
+        s->refined_leaves = img.refined_leaves;
         gshade.resize(n);
         for (uint64_t i = 0; i < n; i++) {
             GShade &g = gshade[i];

@@ -22,7 +22,8 @@
 namespace pray_gpu {
 
 constexpr uint32_t kLeafFlag = 0x80000000u;
-constexpr int kMaxTreeDepth = 30;  // traversal stack bound; builders reject deeper limits
+constexpr int kMaxTreeDepth = 30;        // deepest reference tree the API accepts
+constexpr int kMaxTraversalDepth = 62;   // deepest device hierarchy (reference tree + leaf refinement)
 
 struct alignas(16) GNode {
     float lo[3];

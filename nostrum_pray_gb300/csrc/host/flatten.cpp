@@ -1,0 +1,195 @@
+#include "flatten.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <utility>
+
+namespace pray_gpu {
+
+namespace {
+
+constexpr float kPadRel = 1.0f / 65536.0f;
+// deepest node the flattened hierarchy may have (the kernels' traversal stack
+// holds one entry per level)
+constexpr int kMaxDeviceDepth = kMaxTraversalDepth;
+
+struct Item {
+    uint32_t pos;  // depth-first position of the reference (tie-break key)
+    uint32_t tri;  // triangle id
+};
+
+struct Flattener {
+    const BuiltTree &t;
+    const std::vector<TriPre> &pre;
+    int refine;
+    DeviceImage &out;
+
+    uint32_t alloc_pair() {
+        const uint32_t pair = (uint32_t)out.nodes.size();
+        out.nodes.resize(out.nodes.size() + 2);
+        return pair;
+    }
+
+    void put_tri(const Item &it) {
+        const TriPre &p = pre[it.tri];
+        GTri g;
+        uint32_t idbits = it.tri, key = it.pos;
+        float idf, keyf;
+        std::memcpy(&idf, &idbits, 4);
+        std::memcpy(&keyf, &key, 4);
+        g.v0[0] = p.a[0], g.v0[1] = p.a[1], g.v0[2] = p.a[2], g.v0[3] = idf;
+        g.e1[0] = p.ab[0], g.e1[1] = p.ab[1], g.e1[2] = p.ab[2], g.e1[3] = keyf;
+        g.e2[0] = p.ac[0], g.e2[1] = p.ac[1], g.e2[2] = p.ac[2], g.e2[3] = 0.f;
+        out.tris.push_back(g);
+    }
+
+    // Linear leaf over items[lo, hi) in their current order.
+    void linear_leaf(GNode &g, const std::vector<Item> &items, size_t lo, size_t hi) {
+        g.a = (uint32_t)out.tris.size();
+        g.b = kLeafFlag | (uint32_t)(hi - lo);
+        for (size_t i = lo; i < hi; i++) put_tri(items[i]);
+    }
+
+    // Padded bounds of the triangles items[lo, hi).
+    void padded_box(const std::vector<Item> &items, size_t lo, size_t hi, float blo[3], float bhi[3]) {
+        for (int k = 0; k < 3; k++) blo[k] = INFINITY, bhi[k] = -INFINITY;
+        for (size_t i = lo; i < hi; i++) {
+            const Aabb &b = pre[items[i].tri].box;
+            for (int k = 0; k < 3; k++) blo[k] = std::min(blo[k], b.lo[k]), bhi[k] = std::max(bhi[k], b.hi[k]);
+        }
+        for (int k = 0; k < 3; k++) {
+            const float pad = (std::fabs(blo[k]) + std::fabs(bhi[k]) + (bhi[k] - blo[k])) * kPadRel + 1e-30f;
+            blo[k] -= pad;
+            bhi[k] += pad;
+        }
+    }
+
+    // Median split of items[lo, hi) along the longest axis of the centroid
+    // bounds; the halves become a new node pair, whose index is returned.
+    uint32_t split_pair(std::vector<Item> &items, size_t lo, size_t hi, int depth) {
+        float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (size_t i = lo; i < hi; i++)
+            for (int k = 0; k < 3; k++) {
+                const float c = pre[items[i].tri].mid[k];
+                clo[k] = std::min(clo[k], c);
+                chi[k] = std::max(chi[k], c);
+            }
+        int axis = 0;
+        for (int k = 1; k < 3; k++)
+            if (chi[k] - clo[k] > chi[axis] - clo[axis]) axis = k;
+        const size_t mid = lo + (hi - lo) / 2;
+        std::nth_element(items.begin() + lo, items.begin() + mid, items.begin() + hi,
+                         [&](const Item &x, const Item &y) {
+                             const float a = pre[x.tri].mid[axis], b = pre[y.tri].mid[axis];
+                             return a < b || (a == b && x.pos < y.pos);
+                         });
+        const uint32_t pair = alloc_pair();
+        out.sub_nodes += 2;
+        sub_tree(items, lo, mid, pair, depth + 1);
+        sub_tree(items, mid, hi, pair + 1, depth + 1);
+        return pair;
+    }
+
+    // Sub-hierarchy node over items[lo, hi) (padded box) written into slot.
+    void sub_tree(std::vector<Item> &items, size_t lo, size_t hi, uint32_t slot, int depth) {
+        GNode g;
+        padded_box(items, lo, hi, g.lo, g.hi);
+        if ((int64_t)(hi - lo) <= refine || depth >= kMaxDeviceDepth) {
+            linear_leaf(g, items, lo, hi);
+            out.nodes[slot] = g;
+            return;
+        }
+        g.a = 0;
+        g.b = 0;
+        out.nodes[slot] = g;
+        const uint32_t pair = split_pair(items, lo, hi, depth);
+        out.nodes[slot].a = pair;
+    }
+
+    // Reference node p into slot (the box is the reference's, unpadded).
+    void put(int32_t p, uint32_t slot, int depth) {
+        const FlatNode &n = t.nodes[p];
+        GNode g;
+        for (int k = 0; k < 3; k++) g.lo[k] = n.box.lo[k], g.hi[k] = n.box.hi[k];
+        g.a = 0;
+        g.b = 0;
+        if (n.left < 0) {
+            std::vector<Item> items(n.count);
+            for (uint32_t i = 0; i < n.count; i++) items[i] = Item{n.first + i, t.refs[n.first + i]};
+            if (refine <= 0 || (int64_t)n.count <= refine || depth >= kMaxDeviceDepth) {
+                linear_leaf(g, items, 0, items.size());
+                out.nodes[slot] = g;
+                return;
+            }
+            out.refined_leaves++;
+            out.nodes[slot] = g;
+            const uint32_t pair = split_pair(items, 0, items.size(), depth);
+            out.nodes[slot].a = pair;
+            return;
+        }
+        out.nodes[slot] = g;
+        const uint32_t pair = alloc_pair();
+        out.nodes[slot].a = pair;
+        put(n.left, pair, depth + 1);
+        put(n.right, pair + 1, depth + 1);
+    }
+};
+
+}  // namespace
+
+void flatten_for_device(const BuiltTree &t, const std::vector<TriPre> &pre, int leaf_refine, DeviceImage &out) {
+    out.nodes.assign(2, GNode{});
+    out.tris.clear();
+    out.tris.reserve(t.refs.size());
+    out.refined_leaves = 0;
+    out.sub_nodes = 0;
+    Flattener f{t, pre, leaf_refine, out};
+    f.put(0, 0, 0);
+}
+
+bool validate_device_image(const DeviceImage &img, std::string &why) {
+    const uint64_t nn = img.nodes.size(), nt = img.tris.size();
+    if (nn < 2) {
+        why = "device image has no root";
+        return false;
+    }
+    // iterative walk from the root: every child pair and leaf range in
+    // bounds, every node reached once, depth within the traversal stack
+    std::vector<uint8_t> seen(nn, 0);
+    std::vector<std::pair<uint32_t, int>> todo{{0u, 0}};
+    seen[0] = 1;
+    while (!todo.empty()) {
+        const auto [i, d] = todo.back();
+        todo.pop_back();
+        if (d > kMaxTraversalDepth) {
+            why = "device hierarchy deeper than the traversal stack";
+            return false;
+        }
+        const GNode &g = img.nodes[i];
+        if (g.b & kLeafFlag) {
+            const uint64_t cnt = g.b & ~kLeafFlag;
+            if ((uint64_t)g.a + cnt > nt) {
+                why = "leaf range out of bounds";
+                return false;
+            }
+            continue;
+        }
+        if (g.b != 0 || (g.a & 1u) || (uint64_t)g.a + 1 >= nn || g.a < 2) {
+            why = "child pair out of bounds";
+            return false;
+        }
+        for (uint32_t c = g.a; c <= g.a + 1; c++) {
+            if (seen[c]) {
+                why = "node reached twice";
+                return false;
+            }
+            seen[c] = 1;
+            todo.push_back({c, d + 1});
+        }
+    }
+    return true;
+}
+
+}  // namespace pray_gpu

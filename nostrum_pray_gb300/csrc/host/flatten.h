@@ -1,0 +1,40 @@
+// Flattening of a built tree into the device layout (device_layout.h).
+//
+// The reference's tree is copied node for node: its boxes are tested on the
+// GPU with the reference's slab arithmetic, so the GPU visits exactly the
+// leaves the reference's depth-first traversal would reach. Large leaves of
+// that tree (more than `leaf_refine` references) are then refined into a small
+// bounding-volume hierarchy over their own triangles, whose boxes are the
+// triangles' bounds padded by a relative 2^-16: a ray skips a sub-box only if
+// it cannot come within that pad of any triangle inside, so every triangle the
+// one-sided Moeller-Trumbore test could report as hit is still tested. Each
+// triangle record keeps its depth-first position in the reference's leaf order
+// as the tie-break key, so the refined leaves return the same triangle as a
+// linear scan in the reference's order.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../device_layout.h"
+#include "geom.h"
+#include "kdtree.h"
+
+namespace pray_gpu {
+
+struct DeviceImage {
+    std::vector<GNode> nodes;
+    std::vector<GTri> tris;
+    uint64_t refined_leaves = 0;  // reference leaves split into a sub-hierarchy
+    uint64_t sub_nodes = 0;       // nodes added by the refinement
+};
+
+// leaf_refine <= 0 keeps every reference leaf as one linear leaf.
+void flatten_for_device(const BuiltTree &t, const std::vector<TriPre> &pre, int leaf_refine, DeviceImage &out);
+
+// Structural check before upload: child pairs and leaf ranges in bounds, each
+// node reached once, depth within the kernels' traversal stack.
+bool validate_device_image(const DeviceImage &img, std::string &why);
+
+}  // namespace pray_gpu

@@ -28,8 +28,8 @@ namespace pray_gpu {
 namespace dev {
 
 constexpr float kPruneRel = 1.0f + 1.0f / 4096.0f;
-constexpr int kStack = 32;
-static_assert(kStack > kMaxTreeDepth, "stack must hold a full root-to-leaf path");
+constexpr int kStack = 64;
+static_assert(kStack > kMaxTraversalDepth, "stack must hold a full root-to-leaf path");
 
 struct RayF {
     float ox, oy, oz;
@@ -102,6 +102,7 @@ __device__ __forceinline__ int traverse(const DevScene &s, const RayF &r, float 
                                         FetchCount *fc = nullptr) {
     best_t = FLT_MAX;
     int best = -1;
+    uint32_t best_key = 0xFFFFFFFFu;
     float tn, tf;
     const float4 rlo = ldg4(s.nodes[0].lo), rhi = ldg4(s.nodes[0].hi);
     if (!slab(rlo, rhi, r, tn, tf)) return -1;
@@ -122,10 +123,15 @@ __device__ __forceinline__ int traverse(const DevScene &s, const RayF &r, float 
                 if (intersect_tri(v0, e1, e2, r, eps, t) && t > 0) {
                     if (kAny) {
                         if (d2 > t * t) return (int)i;
-                    } else if (t < best_t || (best >= 0 && t == best_t && (int)i < best)) {
-                        best_t = t;
-                        best = (int)i;
-                        limit = t * kPruneRel;
+                    } else {
+                        // depth-first position in the reference's leaf order
+                        const uint32_t key = __float_as_uint(e1.w);
+                        if (t < best_t || (best >= 0 && t == best_t && key < best_key)) {
+                            best_t = t;
+                            best = (int)i;
+                            best_key = key;
+                            limit = t * kPruneRel;
+                        }
                     }
                 }
             }

@@ -34,7 +34,7 @@ _f32 = ctypes.c_float
 
 class TreeOptions(ctypes.Structure):
     _fields_ = [("tree", _i32), ("leaf_size", _i32), ("max_depth", _i32), ("sah_traversal_cost", _f32),
-                ("sah_intersection_cost", _f32), ("build_threads", _i32)]
+                ("sah_intersection_cost", _f32), ("build_threads", _i32), ("leaf_refine", _i32)]
 
 
 class RtParams(ctypes.Structure):
@@ -60,6 +60,7 @@ _lib = None
 EXPORTED = [
     "pray_last_error", "pray_api_version", "pray_tree_options_default", "pray_host_tree_build",
     "pray_host_tree_destroy", "pray_host_tree_stats", "pray_host_tree_dump", "pray_host_tree_precompute",
+    "pray_host_tree_device_layout",
     "pray_camera", "pray_scene_create", "pray_scene_destroy", "pray_scene_stats", "pray_trace_closest",
     "pray_render_rt", "pray_render_rt_host", "pray_render_rt_counts", "pray_render_pt", "pray_render_pt_host",
 ]
@@ -80,6 +81,7 @@ def lib():
         L.pray_host_tree_stats.argtypes = [_vp, _vp]
         L.pray_host_tree_dump.argtypes = [_vp, _vp, _vp, _vp, _vp]
         L.pray_host_tree_precompute.argtypes = [_vp, _vp]
+        L.pray_host_tree_device_layout.argtypes = [_vp, _i32, _vp]
         L.pray_camera.argtypes = [_u64, _u64, _u64, _vp, _vp, _vp]
         L.pray_scene_create.argtypes = [_vp, _vp, _vp, _u64, ctypes.POINTER(TreeOptions), _i32, ctypes.POINTER(_vp)]
         L.pray_scene_destroy.argtypes = [_vp]
@@ -190,6 +192,12 @@ class HostTree:
     def precompute(self) -> np.ndarray:
         out = np.empty((self.n, 18), np.float32)
         check(lib().pray_host_tree_precompute(self._h, out.ctypes.data))
+        return out
+
+    def device_layout(self, leaf_refine: int = 4) -> np.ndarray:
+        """[node records, triangle references, refined leaves, added nodes]."""
+        out = np.zeros(4, np.uint64)
+        check(lib().pray_host_tree_device_layout(self._h, leaf_refine, out.ctypes.data))
         return out
 
 

@@ -140,3 +140,17 @@ def test_bad_tree_options_rejected():
     for kw in ({"max_depth": 31}, {"leaf_size": 0}, {"tree": 7}, {"sah_intersection_cost": 0.0}):
         with pytest.raises(native.PrayError):
             native.HostTree(m, native.tree_options(**kw))
+
+
+@pytest.mark.parametrize("refine", [0, 1, 4, 16])
+def test_device_layout_valid(refine):
+    for mesh, st in ((scenes.soup(10_000, 0), scenes.soup_setup()), (scenes.icosphere(5), scenes.icosphere_setup()),
+                     (scenes.room(grid=8), scenes.room_setup())):
+        t = native.HostTree(mesh, native.tree_options(st))
+        nodes, refs, refined, added = (int(x) for x in t.device_layout(refine))
+        st_ = t.tree_stats()
+        assert refs == int(st_[4])  # every reference kept exactly once
+        if refine == 0:
+            assert refined == 0 and added == 0 and nodes == int(st_[0]) + 1
+        else:
+            assert nodes == int(st_[0]) + 1 + added
