@@ -77,6 +77,12 @@ typedef enum {
     PRAY_PT_NEE = 1       /* next-event estimation + Russian roulette (no reference counterpart) */
 } pray_pt_mode;
 
+typedef enum {
+    PRAY_SCHED_PIXEL = 0,      /* one thread per pixel, samples and bounces in a loop */
+    PRAY_SCHED_WAVEFRONT = 1   /* path pool + extend / shade / occlusion passes with compacted queues,
+                                  one CUDA graph per frame; PRAY_PT_NEE only */
+} pray_pt_scheduler;
+
 typedef struct {
     uint64_t width, height;
     uint64_t fov;
@@ -89,6 +95,10 @@ typedef struct {
     float det_epsilon;
     int32_t mode;                  /* pray_pt_mode */
     uint32_t rr_depth;             /* PRAY_PT_NEE: Russian roulette from this depth */
+    int32_t scheduler;             /* pray_pt_scheduler */
+    uint32_t sample_offset;        /* first sample index of this call (continues PCG streams across calls) */
+    uint32_t wavefront_paths;      /* PRAY_SCHED_WAVEFRONT: paths in flight per round (0 = 2^23; at least
+                                      one per pixel); a frame runs ceil(spp / (paths / pixels)) rounds */
 } pray_pt_params;
 
 typedef struct pray_scene pray_scene;
@@ -176,6 +186,22 @@ pray_status pray_render_pt(pray_scene *s, const pray_pt_params *p, uint8_t *rgb_
  * may be NULL. Synchronises. */
 pray_status pray_render_pt_host(pray_scene *s, const pray_pt_params *p, uint8_t *rgb_host, float *radiance_host,
                                 uint64_t *rays_cast);
+
+/* FP64 accumulation for converged references: adds the radiance of samples
+ * [sample_offset, sample_offset + num_samples) of every pixel to sum_dev
+ * (height x width x 3 doubles, caller-initialised), one sample at a time in
+ * sample order, so repeated calls over consecutive sample ranges give the
+ * same sums as one call. Device pointers; enqueued on `stream`. */
+pray_status pray_accumulate_pt(pray_scene *s, const pray_pt_params *p, double *sum_dev,
+                               unsigned long long *counters_dev, void *stream);
+
+/* Relative mean squared error of an image against a reference, reduced in
+ * FP64 on the device: mean over pixels and channels of
+ * (x - r)^2 / (r^2 + 0.01), with x = img_scale * img[i], r = ref_scale * ref[i]
+ * (the scales turn sums into means). n = values (pixels x 3). out_dev: one
+ * double. */
+pray_status pray_relmse(const double *img_dev, double img_scale, const double *ref_dev, double ref_scale,
+                        uint64_t n, double *out_dev, void *stream);
 
 #ifdef __cplusplus
 }

@@ -4,6 +4,7 @@
 
 #include <cfloat>
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <exception>
 #include <memory>
@@ -97,6 +98,17 @@ struct pray_scene {
     uint64_t refined_leaves = 0;
     float tol = 0.f;
     uint64_t device_bytes = 0;
+    // wavefront path tracer: scratch (path pool, queues), private stream,
+    // events and the captured frame graph
+    void *d_wf = nullptr;
+    uint64_t wf_bytes = 0;
+    uint64_t wf_capacity = 0, wf_pixels = 0;
+    cudaStream_t wf_stream = nullptr;
+    cudaEvent_t wf_ev_in = nullptr, wf_ev_out = nullptr;
+    cudaGraphExec_t wf_exec = nullptr;
+    PtLaunch wf_key;
+    uint64_t wf_key_cap = 0;
+    int sm_count = 0;
     // frame buffers of the host-memory entry points, grown on demand
     uint8_t *d_rgb = nullptr;
     uint64_t rgb_cap = 0;
@@ -125,6 +137,13 @@ struct pray_scene {
         cudaFree(d_counters);
         cudaFree(d_emit);
         cudaFree(d_emit_cdf);
+        cudaFree(d_wf);
+        if (wf_exec) cudaGraphExecDestroy(wf_exec);
+        if (wf_stream) cudaStreamDestroy(wf_stream);
+        if (wf_ev_in) cudaEventDestroy(wf_ev_in);
+        if (wf_ev_out) cudaEventDestroy(wf_ev_out);
+        d_wf = nullptr, wf_exec = nullptr, wf_stream = nullptr, wf_ev_in = nullptr, wf_ev_out = nullptr;
+        wf_bytes = 0;
         d_nodes = nullptr, d_tris = nullptr, d_shade = nullptr, d_rgb = nullptr, d_counters = nullptr;
         d_emit = nullptr, d_emit_cdf = nullptr;
     }
@@ -182,6 +201,12 @@ pray_status check_pt_params(const pray_pt_params *p) {
         return set_error(PRAY_ERR_UNSUPPORTED, "max_depth must be below 64");
     if (p->mode != PRAY_PT_KAJIYA && p->mode != PRAY_PT_NEE)
         return set_error(PRAY_ERR_INVALID_ARGUMENT, "mode must be PRAY_PT_KAJIYA or PRAY_PT_NEE");
+    if (p->scheduler != PRAY_SCHED_PIXEL && p->scheduler != PRAY_SCHED_WAVEFRONT)
+        return set_error(PRAY_ERR_INVALID_ARGUMENT, "scheduler must be PRAY_SCHED_PIXEL or PRAY_SCHED_WAVEFRONT");
+    if (p->scheduler == PRAY_SCHED_WAVEFRONT && p->mode != PRAY_PT_NEE)
+        return set_error(PRAY_ERR_UNSUPPORTED, "the wavefront scheduler runs PRAY_PT_NEE only");
+    if ((uint64_t)p->sample_offset + p->num_samples > 0xFFFFFFFFull)
+        return set_error(PRAY_ERR_INVALID_ARGUMENT, "sample_offset + num_samples must fit in 32 bits");
     return PRAY_OK;
 }
 
@@ -196,6 +221,7 @@ PtLaunch make_pt_launch(const pray_pt_params *p) {
     L.mode = p->mode;
     L.seed = p->seed;
     L.eps = p->det_epsilon;
+    L.sample_offset = p->sample_offset;
     return L;
 }
 
@@ -227,6 +253,77 @@ pray_status ensure_frame(pray_scene *s, uint64_t bytes) {
     }
     if (!s->d_counters && (e = cudaMalloc(&s->d_counters, 8 * sizeof(unsigned long long))) != cudaSuccess)
         return cuda_error(e, "cudaMalloc (counters)");
+    return PRAY_OK;
+}
+
+// Most paths a wavefront round keeps in flight (at least one per pixel).
+constexpr uint64_t kWavefrontMaxPaths = 1ull << 23;
+
+// Runs a path-tracing launch with the chosen scheduler on `stream`.
+pray_status run_pt(pray_scene *s, const PtLaunch &L, int scheduler, uint32_t wavefront_paths, cudaStream_t stream) {
+    cudaError_t e;
+    if (scheduler == PRAY_SCHED_PIXEL) {
+        e = launch_render_pt(s->view(), L, stream);
+        return e == cudaSuccess ? PRAY_OK : cuda_error(e, "render_pt launch");
+    }
+    const uint64_t P = (uint64_t)L.cam.width * L.cam.height;
+    const uint64_t max_paths = wavefront_paths ? wavefront_paths : kWavefrontMaxPaths;
+    const uint64_t cap = std::max<uint64_t>(P, std::min<uint64_t>(P * L.num_samples, max_paths));
+    if (cap >= (1ull << 32)) return set_error(PRAY_ERR_UNSUPPORTED, "frame too large for the wavefront scheduler");
+    if (!s->wf_stream) {
+        if ((e = cudaStreamCreateWithFlags(&s->wf_stream, cudaStreamNonBlocking)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&s->wf_ev_in, cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&s->wf_ev_out, cudaEventDisableTiming)) != cudaSuccess)
+            return cuda_error(e, "wavefront stream set-up");
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    }
+    if (s->wf_capacity < cap || s->wf_pixels < P) {
+        const uint64_t ncap = std::max(cap, s->wf_capacity), npx = std::max(P, s->wf_pixels);
+        const uint64_t bytes = wavefront_scratch_bytes(ncap, npx);
+        if ((e = cudaStreamSynchronize(s->wf_stream)) != cudaSuccess) return cuda_error(e, "wavefront sync");
+        cudaFree(s->d_wf);
+        s->d_wf = nullptr;
+        s->wf_capacity = s->wf_pixels = 0;
+        if ((e = cudaMalloc(&s->d_wf, bytes)) != cudaSuccess) return cuda_error(e, "cudaMalloc (wavefront)");
+        s->wf_capacity = ncap;
+        s->wf_pixels = npx;
+        s->wf_bytes = bytes;
+        if (s->wf_exec) cudaGraphExecDestroy(s->wf_exec);
+        s->wf_exec = nullptr;
+    }
+    if (!s->wf_exec || std::memcmp(&s->wf_key, &L, sizeof(L)) != 0 || s->wf_key_cap != cap) {
+        if (s->wf_exec) cudaGraphExecDestroy(s->wf_exec);
+        s->wf_exec = nullptr;
+        WavefrontScratch w = wavefront_carve(s->d_wf, s->wf_capacity, s->wf_pixels);
+        w.capacity = cap;
+        cudaGraph_t g = nullptr;
+        if ((e = cudaStreamBeginCapture(s->wf_stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+            return cuda_error(e, "graph capture");
+        cudaError_t le = record_wavefront_frame(s->view(), L, w, s->sm_count, s->wf_stream);
+        e = cudaStreamEndCapture(s->wf_stream, &g);
+        if (le != cudaSuccess || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return cuda_error(le != cudaSuccess ? le : e, "wavefront capture");
+        }
+        e = cudaGraphInstantiate(&s->wf_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            s->wf_exec = nullptr;
+            return cuda_error(e, "graph instantiate");
+        }
+        std::memcpy(&s->wf_key, &L, sizeof(L));
+        s->wf_key_cap = cap;
+    }
+    // order the private stream after the caller's work, and the caller's
+    // later work after the frame
+    if ((e = cudaEventRecord(s->wf_ev_in, stream)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(s->wf_stream, s->wf_ev_in, 0)) != cudaSuccess ||
+        (e = cudaGraphLaunch(s->wf_exec, s->wf_stream)) != cudaSuccess ||
+        (e = cudaEventRecord(s->wf_ev_out, s->wf_stream)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(stream, s->wf_ev_out, 0)) != cudaSuccess)
+        return cuda_error(e, "wavefront launch");
     return PRAY_OK;
 }
 
@@ -528,9 +625,27 @@ pray_status pray_render_pt(pray_scene *s, const pray_pt_params *p, uint8_t *rgb,
     L.rgb = rgb;
     L.radiance = radiance;
     L.counters = counters;
-    e = launch_render_pt(s->view(), L, (cudaStream_t)stream);
-    if (e != cudaSuccess) return cuda_error(e, "render_pt launch");
-    return PRAY_OK;
+    return run_pt(s, L, p->scheduler, p->wavefront_paths, (cudaStream_t)stream);
+}
+
+pray_status pray_accumulate_pt(pray_scene *s, const pray_pt_params *p, double *sum, unsigned long long *counters,
+                               void *stream) {
+    if (!s || !sum) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    pray_status st = check_pt_params(p);
+    if (st != PRAY_OK) return st;
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    PtLaunch L = make_pt_launch(p);
+    L.sum64 = sum;
+    L.counters = counters;
+    return run_pt(s, L, p->scheduler, p->wavefront_paths, (cudaStream_t)stream);
+}
+
+pray_status pray_relmse(const double *img, double img_scale, const double *ref, double ref_scale, uint64_t n,
+                        double *out, void *stream) {
+    if (!img || !ref || !out) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    cudaError_t e = launch_relmse(img, img_scale, ref, ref_scale, n, out, (cudaStream_t)stream);
+    return e == cudaSuccess ? PRAY_OK : cuda_error(e, "relmse launch");
 }
 
 pray_status pray_render_pt_host(pray_scene *s, const pray_pt_params *p, uint8_t *rgb_host, float *radiance_host,
@@ -548,7 +663,7 @@ pray_status pray_render_pt_host(pray_scene *s, const pray_pt_params *p, uint8_t 
     L.rgb = s->d_rgb;
     L.radiance = radiance_host ? reinterpret_cast<float *>(s->d_rgb + ((3 * px + 15) & ~15ull)) : nullptr;
     L.counters = s->d_counters;
-    if ((e = launch_render_pt(s->view(), L, 0)) != cudaSuccess) return cuda_error(e, "render_pt launch");
+    if ((st = run_pt(s, L, p->scheduler, p->wavefront_paths, 0)) != PRAY_OK) return st;
     if ((e = cudaMemcpy(rgb_host, s->d_rgb, 3 * px, cudaMemcpyDeviceToHost)) != cudaSuccess)
         return cuda_error(e, "cudaMemcpy (frame)");
     if (radiance_host &&

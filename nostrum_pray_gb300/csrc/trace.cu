@@ -20,65 +20,81 @@ __global__ void __launch_bounds__(128) k_trace_closest(DevScene s, const float *
                                                        float eps, int32_t *__restrict__ ids,
                                                        float *__restrict__ ts) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float *p = rays + 9 * i;
-    RayF r;
-    r.ox = p[0], r.oy = p[1], r.oz = p[2];
-    r.dx = p[3], r.dy = p[4], r.dz = p[5];
-    r.ix = p[6], r.iy = p[7], r.iz = p[8];
+    const bool valid = i < n;
+    RayF r{};
+    if (valid) {
+        const float *p = rays + 9 * i;
+        r.ox = p[0], r.oy = p[1], r.oz = p[2];
+        r.dx = p[3], r.dy = p[4], r.dz = p[5];
+        r.ix = p[6], r.iy = p[7], r.iz = p[8];
+    }
     float t;
-    const int pos = traverse<false>(s, r, eps, 0.f, t);
-    ids[i] = pos >= 0 ? (int32_t)__float_as_uint(__ldg(&s.tris[pos].v0[3])) : -1;
-    ts[i] = t;
+    const int pos = traverse<false>(s, r, eps, 0.f, valid && s.n_refs > 0, t);
+    if (valid) {
+        ids[i] = pos >= 0 ? (int32_t)__float_as_uint(__ldg(&s.tris[pos].v0[3])) : -1;
+        ts[i] = t;
+    }
 }
 
 // Fused ray-tracing render: primary ray, closest hit, per-light Lambert with
 // an occlusion ray, clamp and quantise (evaluateRay, src/pray.cpp:17-55, and
-// the quantisation of src/pray.cpp:576-588).
+// the quantisation of src/pray.cpp:576-588). Every lane of a warp runs the
+// same light loop so that the warp-collective traversals line up; a lane
+// whose colour saturated stops casting (the reference's early break).
 template <bool kCount>
 __global__ void __launch_bounds__(128) k_render_rt(DevScene s, RtLaunch L) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t px, py;
     const bool active = pixel_of(i, L.cam.width, L.cam.height, px, py);
     uint32_t shadows = 0;
-    bool shaded = false;
     FetchCount fc;
-    if (active) {
-        const RayF r = primary_ray(L.cam, px, py);
-        float cr = L.bg[0], cg = L.bg[1], cb = L.bg[2];
-        float dist = FLT_MAX;
-        const int pos = (s.n_refs > 0) ? traverse<false, kCount>(s, r, L.eps, 0.f, dist, &fc) : -1;
-        int32_t id = -1;
-        shaded = pos >= 0;
-        if (pos >= 0) {
-            id = (int32_t)__float_as_uint(__ldg(&s.tris[pos].v0[3]));
-            const float4 nrm = __ldg(reinterpret_cast<const float4 *>(s.shade[id].n));
-            const float4 alb = __ldg(reinterpret_cast<const float4 *>(s.shade[id].c));
-            const float hx = r.ox + r.dx * dist, hy = r.oy + r.dy * dist, hz = r.oz + r.dz * dist;
-            cr = 0.f, cg = 0.f, cb = 0.f;
-            for (int l = 0; l < L.n_lights; l++) {
-                float lx = L.lights[l][0] - hx, ly = L.lights[l][1] - hy, lz = L.lights[l][2] - hz;
-                const float d2 = lx * lx + ly * ly + lz * lz;
-                if (d2 > 0) {
-                    const float inv = 1.0f / sqrtf(d2);
-                    lx *= inv, ly *= inv, lz *= inv;
-                }
-                const float lambert = lx * nrm.x + ly * nrm.y + lz * nrm.z;
-                if (lambert < 0.f) continue;
-                shadows++;
-                const RayF sr = make_ray(hx, hy, hz, lx, ly, lz);
-                float dummy;
-                if (traverse<true, kCount>(s, sr, L.eps, d2, dummy, &fc) >= 0) continue;
-                const float w = 1.0f / d2;
-                cr = cr + ((alb.x * L.lights[l][3]) * lambert) * w;
-                cg = cg + ((alb.y * L.lights[l][4]) * lambert) * w;
-                cb = cb + ((alb.z * L.lights[l][5]) * lambert) * w;
-                if (cr >= 1.f && cg >= 1.f && cb >= 1.f) break;
+    const RayF r = primary_ray(L.cam, active ? px : 0, active ? py : 0);
+    float dist = FLT_MAX;
+    const int pos = traverse<false, kCount>(s, r, L.eps, 0.f, active && s.n_refs > 0, dist, &fc);
+    const bool hit = active && pos >= 0;
+    float cr = L.bg[0], cg = L.bg[1], cb = L.bg[2];
+    int32_t id = -1;
+    float4 nrm = make_float4(0.f, 0.f, 0.f, 0.f), alb = nrm;
+    float hx = 0.f, hy = 0.f, hz = 0.f;
+    if (hit) {
+        id = (int32_t)__float_as_uint(__ldg(&s.tris[pos].v0[3]));
+        nrm = __ldg(reinterpret_cast<const float4 *>(s.shade[id].n));
+        alb = __ldg(reinterpret_cast<const float4 *>(s.shade[id].c));
+        hx = r.ox + r.dx * dist, hy = r.oy + r.dy * dist, hz = r.oz + r.dz * dist;
+        cr = 0.f, cg = 0.f, cb = 0.f;
+    }
+    bool done = !hit;
+    for (int l = 0; l < L.n_lights; l++) {
+        float lx = 0.f, ly = 0.f, lz = 0.f, d2 = 0.f, lambert = 0.f;
+        bool need = false;
+        if (!done) {
+            lx = L.lights[l][0] - hx, ly = L.lights[l][1] - hy, lz = L.lights[l][2] - hz;
+            d2 = lx * lx + ly * ly + lz * lz;
+            if (d2 > 0) {
+                const float inv = 1.0f / sqrtf(d2);
+                lx *= inv, ly *= inv, lz *= inv;
             }
-            cr = smax(0.f, smin(1.f, cr));
-            cg = smax(0.f, smin(1.f, cg));
-            cb = smax(0.f, smin(1.f, cb));
+            lambert = lx * nrm.x + ly * nrm.y + lz * nrm.z;
+            need = !(lambert < 0.f);
         }
+        const RayF sr = need ? make_ray(hx, hy, hz, lx, ly, lz) : r;
+        shadows += need ? 1u : 0u;
+        float dummy;
+        const bool occluded = traverse<true, kCount>(s, sr, L.eps, d2, need, dummy, &fc) >= 0;
+        if (need && !occluded) {
+            const float w = 1.0f / d2;
+            cr = cr + ((alb.x * L.lights[l][3]) * lambert) * w;
+            cg = cg + ((alb.y * L.lights[l][4]) * lambert) * w;
+            cb = cb + ((alb.z * L.lights[l][5]) * lambert) * w;
+            if (cr >= 1.f && cg >= 1.f && cb >= 1.f) done = true;
+        }
+    }
+    if (hit) {
+        cr = smax(0.f, smin(1.f, cr));
+        cg = smax(0.f, smin(1.f, cg));
+        cb = smax(0.f, smin(1.f, cb));
+    }
+    if (active) {
         uint8_t *o = L.rgb + 3ull * ((uint64_t)py * L.cam.width + px);
         o[0] = (uint8_t)quantise(cr);
         o[1] = (uint8_t)quantise(cg);
@@ -101,7 +117,7 @@ __global__ void __launch_bounds__(128) k_render_rt(DevScene s, RtLaunch L) {
         if (kCount) {
             // node-pair fetches, triangle-reference fetches, shaded hits
             unsigned long long pairs = fc.pairs, tris = fc.tris;
-            const uint32_t hits = __popc(__ballot_sync(0xFFFFFFFFu, active && shaded));
+            const uint32_t hits = __popc(__ballot_sync(0xFFFFFFFFu, hit));
             for (int o = 16; o > 0; o >>= 1) {
                 pairs += __shfl_xor_sync(0xFFFFFFFFu, pairs, o);
                 tris += __shfl_xor_sync(0xFFFFFFFFu, tris, o);

@@ -36,12 +36,39 @@ struct PtLaunch {
     int32_t mode;                    // 0: reference recursion, 1: NEE + Russian roulette
     uint64_t seed;
     float eps;
-    uint8_t *rgb;                    // out: height x width x 3
+    uint32_t sample_offset;          // first sample index (PCG stream selector)
+    uint8_t *rgb;                    // optional out: height x width x 3
     float *radiance;                 // optional out: height x width x 3 mean radiance
+    double *sum64;                   // optional in/out: height x width x 3 FP64 sums, samples added in order
     unsigned long long *counters;    // optional out (accumulated): [0] paths, [1] ray segments
 };
 
 cudaError_t launch_render_pt(const DevScene &s, const PtLaunch &L, cudaStream_t stream);
+
+// Wavefront path tracer (wavefront.cu): path pool and queues in `scratch`.
+struct WavefrontScratch {
+    float4 *org, *dir, *thr, *rad;   // per path: origin, direction, throughput, radiance
+    uint64_t *rng;                   // per path: PCG32 state
+    uint32_t *depth;                 // per path
+    float *hit_t;                    // per path: closest-hit distance
+    int32_t *hit_ref;                // per path: closest-hit reference (-1: miss)
+    uint32_t *queue[2];              // path ids, ping-pong
+    float4 *shadow;                  // occlusion jobs: 3 float4 each (origin+path, dir+dist2, contribution)
+    uint32_t *counts;                // [0], [1]: queue lengths, [2]: occlusion jobs
+    float *pixel_sum;                // per pixel x 3: running float sum over samples
+    uint64_t capacity;               // paths per round
+};
+
+// Bytes of scratch for `capacity` paths and `pixels` pixels.
+uint64_t wavefront_scratch_bytes(uint64_t capacity, uint64_t pixels);
+// Carves a scratch block of wavefront_scratch_bytes() bytes (256-byte aligned base).
+WavefrontScratch wavefront_carve(void *base, uint64_t capacity, uint64_t pixels);
+// Enqueues one whole frame (all rounds) on `stream`; capturable in a graph.
+cudaError_t record_wavefront_frame(const DevScene &s, const PtLaunch &L, const WavefrontScratch &w, int sm_count,
+                                   cudaStream_t stream);
+
+cudaError_t launch_relmse(const double *img, double img_scale, const double *ref, double ref_scale, uint64_t n,
+                          double *out, cudaStream_t stream);
 
 cudaError_t launch_trace_closest(const DevScene &s, const float *rays, uint64_t n, float eps, int32_t *ids,
                                  float *ts, cudaStream_t stream);

@@ -97,83 +97,140 @@ struct FetchCount {
     uint32_t pairs = 0, tris = 0;
 };
 
+// Pops the next stacked node that can still hold a closer hit.
+__device__ __forceinline__ bool pop_node(const uint32_t *stk_a, const uint32_t *stk_b, const float *stk_t, int &sp,
+                                         float limit, uint32_t &a, uint32_t &b, float &tn) {
+    while (sp > 0) {
+        sp--;
+        if (stk_t[sp] <= limit) {
+            a = stk_a[sp];
+            b = stk_b[sp];
+            tn = stk_t[sp];
+            return true;
+        }
+    }
+    return false;
+}
+
+// Warp-collective traversal: every lane of the warp must call it together
+// (inactive lanes pass valid = false). Structure after Aila & Laine,
+// "Understanding the Efficiency of Ray Traversal on GPUs" (HPG 2009): the
+// warp first walks interior nodes until every lane holds a leaf ("postponing"
+// the first leaf it meets and speculatively continuing), then intersects the
+// postponed leaves together, so lanes do the same kind of work at the same
+// time.
+//
+// Closest hit (kAny = false): returns the index of the winning triangle
+// record or -1, its distance in best_t.
+// Any hit (kAny = true): returns >= 0 once a triangle with t > 0 and
+// t * t < d2 is found (the occlusion test of src/pray.cpp:42).
 template <bool kAny, bool kCount = false>
-__device__ __forceinline__ int traverse(const DevScene &s, const RayF &r, float eps, float d2, float &best_t,
-                                        FetchCount *fc = nullptr) {
+__device__ __forceinline__ int traverse(const DevScene &s, const RayF &r, float eps, float d2, bool valid,
+                                        float &best_t, FetchCount *fc = nullptr) {
+    constexpr unsigned kFull = 0xFFFFFFFFu;
     best_t = FLT_MAX;
     int best = -1;
     uint32_t best_key = 0xFFFFFFFFu;
-    float tn, tf;
-    const float4 rlo = ldg4(s.nodes[0].lo), rhi = ldg4(s.nodes[0].hi);
-    if (!slab(rlo, rhi, r, tn, tf)) return -1;
-    uint32_t a = __float_as_uint(rlo.w), b = __float_as_uint(rhi.w);
     float limit = kAny ? sqrtf(d2) * kPruneRel : FLT_MAX;
     const float back = -s.tol;
+    uint32_t a = 0, b = 0, la = 0, lb = 0;
+    float cur_tn = 0.f, leaf_tn = 0.f;
+    bool have_node = false, have_leaf = false;
+    if (valid) {
+        float tn, tf;
+        const float4 rlo = ldg4(s.nodes[0].lo), rhi = ldg4(s.nodes[0].hi);
+        if (slab(rlo, rhi, r, tn, tf)) {
+            a = __float_as_uint(rlo.w);
+            b = __float_as_uint(rhi.w);
+            cur_tn = tn;
+            have_node = true;
+        }
+    }
     uint32_t stk_a[kStack], stk_b[kStack];
     float stk_t[kStack];
     int sp = 0;
-    while (true) {
-        if (b & kLeafFlag) {
-            const uint32_t end = a + (b & ~kLeafFlag);
-            for (uint32_t i = a; i < end; i++) {
-                if (kCount) fc->tris++;
-                const GTri *T = s.tris + i;
-                const float4 v0 = ldg4(T->v0), e1 = ldg4(T->e1), e2 = ldg4(T->e2);
-                float t;
-                if (intersect_tri(v0, e1, e2, r, eps, t) && t > 0) {
-                    if (kAny) {
-                        if (d2 > t * t) return (int)i;
-                    } else {
-                        // depth-first position in the reference's leaf order
-                        const uint32_t key = __float_as_uint(e1.w);
-                        if (t < best_t || (best >= 0 && t == best_t && key < best_key)) {
-                            best_t = t;
-                            best = (int)i;
-                            best_key = key;
-                            limit = t * kPruneRel;
+    while (__any_sync(kFull, have_node || have_leaf)) {
+        // 1. interior nodes, until every lane has found a leaf
+        while (true) {
+            const bool interior = have_node && !(b & kLeafFlag);
+            if (!__any_sync(kFull, interior && !have_leaf)) break;
+            if (interior) {
+                if (kCount) fc->pairs++;
+                const GNode *c = s.nodes + a;
+                const float4 l0 = ldg4(c[0].lo), h0 = ldg4(c[0].hi), l1 = ldg4(c[1].lo), h1 = ldg4(c[1].hi);
+                float tn0, tf0, tn1, tf1;
+                const bool v0 = slab(l0, h0, r, tn0, tf0) && tn0 <= limit && tf0 >= back;
+                const bool v1 = slab(l1, h1, r, tn1, tf1) && tn1 <= limit && tf1 >= back;
+                if (v0 && v1) {
+                    const bool first0 = tn0 <= tn1;
+                    stk_a[sp] = __float_as_uint(first0 ? l1.w : l0.w);
+                    stk_b[sp] = __float_as_uint(first0 ? h1.w : h0.w);
+                    stk_t[sp] = first0 ? tn1 : tn0;
+                    sp++;
+                    a = __float_as_uint(first0 ? l0.w : l1.w);
+                    b = __float_as_uint(first0 ? h0.w : h1.w);
+                    cur_tn = first0 ? tn0 : tn1;
+                } else if (v0 || v1) {
+                    a = __float_as_uint(v0 ? l0.w : l1.w);
+                    b = __float_as_uint(v0 ? h0.w : h1.w);
+                    cur_tn = v0 ? tn0 : tn1;
+                } else {
+                    have_node = pop_node(stk_a, stk_b, stk_t, sp, limit, a, b, cur_tn);
+                }
+                if (have_node && (b & kLeafFlag) && !have_leaf) {
+                    // first leaf: postpone it and keep walking
+                    la = a, lb = b, leaf_tn = cur_tn;
+                    have_leaf = true;
+                    have_node = pop_node(stk_a, stk_b, stk_t, sp, limit, a, b, cur_tn);
+                }
+            }
+        }
+        // 2. leaves: the postponed one, then any leaf the walk stopped on
+        while (true) {
+            const bool work = have_leaf || (have_node && (b & kLeafFlag));
+            if (!__any_sync(kFull, work)) break;
+            if (work) {
+                uint32_t fa, fb;
+                float ftn;
+                if (have_leaf) {
+                    fa = la, fb = lb, ftn = leaf_tn;
+                    have_leaf = false;
+                } else {
+                    fa = a, fb = b, ftn = cur_tn;
+                    have_node = pop_node(stk_a, stk_b, stk_t, sp, limit, a, b, cur_tn);
+                }
+                if (ftn <= limit) {
+                    const uint32_t end = fa + (fb & ~kLeafFlag);
+                    for (uint32_t i = fa; i < end; i++) {
+                        if (kCount) fc->tris++;
+                        const GTri *T = s.tris + i;
+                        const float4 v0 = ldg4(T->v0), e1 = ldg4(T->e1), e2 = ldg4(T->e2);
+                        float t;
+                        if (intersect_tri(v0, e1, e2, r, eps, t) && t > 0) {
+                            if (kAny) {
+                                if (d2 > t * t) {
+                                    best = (int)i;
+                                    have_node = have_leaf = false;
+                                    sp = 0;
+                                    break;
+                                }
+                            } else {
+                                // depth-first position in the reference's leaf order
+                                const uint32_t key = __float_as_uint(e1.w);
+                                if (t < best_t || (best >= 0 && t == best_t && key < best_key)) {
+                                    best_t = t;
+                                    best = (int)i;
+                                    best_key = key;
+                                    limit = t * kPruneRel;
+                                }
+                            }
                         }
                     }
                 }
             }
-        } else {
-            if (kCount) fc->pairs++;
-            const GNode *c = s.nodes + a;
-            const float4 l0 = ldg4(c[0].lo), h0 = ldg4(c[0].hi), l1 = ldg4(c[1].lo), h1 = ldg4(c[1].hi);
-            float tn0, tf0, tn1, tf1;
-            const bool v0 = slab(l0, h0, r, tn0, tf0) && tn0 <= limit && tf0 >= back;
-            const bool v1 = slab(l1, h1, r, tn1, tf1) && tn1 <= limit && tf1 >= back;
-            if (v0 && v1) {
-                const bool first0 = tn0 <= tn1;
-                const float4 nl = first0 ? l0 : l1, nh = first0 ? h0 : h1;
-                const float4 fl = first0 ? l1 : l0, fh = first0 ? h1 : h0;
-                stk_a[sp] = __float_as_uint(fl.w);
-                stk_b[sp] = __float_as_uint(fh.w);
-                stk_t[sp] = first0 ? tn1 : tn0;
-                sp++;
-                a = __float_as_uint(nl.w);
-                b = __float_as_uint(nh.w);
-                continue;
-            }
-            if (v0 || v1) {
-                a = __float_as_uint(v0 ? l0.w : l1.w);
-                b = __float_as_uint(v0 ? h0.w : h1.w);
-                continue;
-            }
         }
-        // pop the next box that can still hold a closer hit
-        bool found = false;
-        while (sp > 0) {
-            sp--;
-            if (stk_t[sp] <= limit) {
-                a = stk_a[sp];
-                b = stk_b[sp];
-                found = true;
-                break;
-            }
-        }
-        if (!found) break;
     }
-    return kAny ? -1 : best;
+    return best;
 }
 
 // Primary ray of pixel (px, py), src/scene_preprocessor.cpp:124-134.

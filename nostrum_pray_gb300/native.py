@@ -25,6 +25,7 @@ CLI_PATH = os.path.join(_PKG, "_build", "Pray")
 PRAY_OK = 0
 TREE_MEDIAN, TREE_SAH = 0, 1
 PT_KAJIYA, PT_NEE = 0, 1
+SCHED_PIXEL, SCHED_WAVEFRONT = 0, 1
 
 _vp = ctypes.c_void_p
 _u64 = ctypes.c_uint64
@@ -47,7 +48,8 @@ class PtParams(ctypes.Structure):
     _fields_ = [("width", _u64), ("height", _u64), ("fov", _u64), ("camera_position", _f32 * 3),
                 ("camera_look", _f32 * 3), ("background", _f32 * 3), ("max_depth", ctypes.c_uint32),
                 ("num_samples", ctypes.c_uint32), ("seed", _u64), ("det_epsilon", _f32), ("mode", _i32),
-                ("rr_depth", ctypes.c_uint32)]
+                ("rr_depth", ctypes.c_uint32), ("scheduler", _i32), ("sample_offset", ctypes.c_uint32),
+                ("wavefront_paths", ctypes.c_uint32)]
 
 
 class PrayError(RuntimeError):
@@ -63,6 +65,7 @@ EXPORTED = [
     "pray_host_tree_device_layout",
     "pray_camera", "pray_scene_create", "pray_scene_destroy", "pray_scene_stats", "pray_trace_closest",
     "pray_render_rt", "pray_render_rt_host", "pray_render_rt_counts", "pray_render_pt", "pray_render_pt_host",
+    "pray_accumulate_pt", "pray_relmse",
 ]
 
 
@@ -92,6 +95,8 @@ def lib():
         L.pray_render_rt_counts.argtypes = [_vp, ctypes.POINTER(RtParams), _vp]
         L.pray_render_pt.argtypes = [_vp, ctypes.POINTER(PtParams), _vp, _vp, _vp, _vp]
         L.pray_render_pt_host.argtypes = [_vp, ctypes.POINTER(PtParams), _vp, _vp, _vp]
+        L.pray_accumulate_pt.argtypes = [_vp, ctypes.POINTER(PtParams), _vp, _vp, _vp]
+        L.pray_relmse.argtypes = [_vp, ctypes.c_double, _vp, ctypes.c_double, _u64, _vp, _vp]
         for name in EXPORTED:
             if not hasattr(L, name):
                 raise PrayError(f"{LIB_PATH} does not export {name}")
@@ -139,7 +144,8 @@ def rt_params(setup) -> Tuple[RtParams, np.ndarray]:
 
 
 def pt_params(setup, spp: Optional[int] = None, max_depth: Optional[int] = None, seed: int = 0,
-              mode: int = PT_KAJIYA, rr_depth: int = 3) -> PtParams:
+              mode: int = PT_KAJIYA, rr_depth: int = 3, scheduler: int = SCHED_PIXEL,
+              sample_offset: int = 0, wavefront_paths: int = 0) -> PtParams:
     p = PtParams()
     p.width, p.height, p.fov = setup.width, setup.height, setup.fov
     p.camera_position[:] = list(setup.cam_pos)
@@ -148,7 +154,14 @@ def pt_params(setup, spp: Optional[int] = None, max_depth: Optional[int] = None,
     p.max_depth = setup.max_depth_pt if max_depth is None else max_depth
     p.num_samples = setup.num_samples if spp is None else spp
     p.seed, p.det_epsilon, p.mode, p.rr_depth = seed, setup.det_eps, mode, rr_depth
+    p.scheduler, p.sample_offset, p.wavefront_paths = scheduler, sample_offset, wavefront_paths
     return p
+
+
+def relmse(img_sum, img_scale: float, ref_sum, ref_scale: float, out, stream=None) -> None:
+    """FP64 relMSE of two device FP64 images (sums scaled to means) into out[0]."""
+    check(lib().pray_relmse(_ptr(img_sum), img_scale, _ptr(ref_sum), ref_scale, img_sum.numel(), _ptr(out),
+                            _stream(stream)))
 
 
 def camera(width, height, fov, cam_pos, cam_look) -> np.ndarray:
@@ -239,6 +252,9 @@ class Scene:
         check(lib().pray_render_rt(self._h, ctypes.byref(p), _ptr(rgb), _ptr(ids), _ptr(ts), _ptr(counters),
                                    _stream(stream)))
         del keep
+
+    def accumulate_pt(self, params: PtParams, sum64, counters=None, stream=None) -> None:
+        check(lib().pray_accumulate_pt(self._h, ctypes.byref(params), _ptr(sum64), _ptr(counters), _stream(stream)))
 
     def render_pt(self, params: PtParams, rgb, radiance=None, counters=None, stream=None) -> None:
         check(lib().pray_render_pt(self._h, ctypes.byref(params), _ptr(rgb), _ptr(radiance), _ptr(counters),

@@ -74,7 +74,7 @@ def lib():
         L.orc_render_pt.restype = _u64
         L.orc_render_pt.argtypes = [_vp, _u64, _u64, _u64, _f32p, _f32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
                                     _u64, ctypes.c_float, ctypes.c_int, ctypes.c_uint32, _u64, _u64, _u8p,
-                                    _vp, ctypes.c_int]
+                                    _vp, ctypes.c_int, ctypes.c_uint32, _vp]
         _lib = L
     return _lib
 
@@ -179,15 +179,20 @@ class OracleScene(_TreeDumpMixin):
         return out, int(nsh)
 
     def render_pt(self, setup, spp: int, max_depth: int, seed: int = 0, mode: int = 0, rr_depth: int = 3,
-                  rows: Optional[Sequence[int]] = None, threads: Optional[int] = None):
-        """Returns (rgb uint8 (rows, width, 3), mean radiance float32, segments)."""
+                  rows: Optional[Sequence[int]] = None, threads: Optional[int] = None, sample_offset: int = 0,
+                  sum64: Optional[np.ndarray] = None):
+        """Returns (rgb uint8 (rows, width, 3), mean radiance float32, segments).
+        sum64 (rows, width, 3) float64, if given, is added to in sample order."""
         r0, r1 = (0, setup.height) if rows is None else rows
         out = np.empty((r1 - r0, setup.width, 3), np.uint8)
         rad = np.empty((r1 - r0, setup.width, 3), np.float32)
+        if sum64 is not None:
+            assert sum64.dtype == np.float64 and sum64.flags.c_contiguous
         segs = lib().orc_render_pt(self._h, setup.width, setup.height, setup.fov, _f3(setup.cam_pos),
                                    _f3(setup.cam_look), _f3(setup.background), max_depth, spp, seed,
                                    setup.det_eps, mode, rr_depth, r0, r1, out, rad.ctypes.data,
-                                   threads or default_threads())
+                                   threads or default_threads(), sample_offset,
+                                   None if sum64 is None else sum64.ctypes.data)
         return out, rad, int(segs)
 
 

@@ -656,10 +656,12 @@ void orc_sample_hemisphere(const float *normals, const float *u, uint64_t n, flo
 
 // Path-traced rows [row0, row1): out_rgb width*(row1-row0)*3 bytes, out_rad
 // (may be NULL) the mean radiance per pixel. Returns the ray segments cast.
+// sample_offset selects the first PCG stream (sample index); out_sum64 (may
+// be NULL) is added to, one sample at a time in sample order, in double.
 uint64_t orc_render_pt(void *h, uint64_t w, uint64_t hh, uint64_t fov, const float *pos, const float *look,
                        const float *bg, uint32_t max_depth, uint32_t spp, uint64_t seed, float eps, int mode,
                        uint32_t rr_depth, uint64_t row0, uint64_t row1, uint8_t *out_rgb, float *out_rad,
-                       int threads) {
+                       int threads, uint32_t sample_offset, double *out_sum64) {
     auto &s = *static_cast<Scene *>(h);
     Camera c = make_camera(w, hh, fov, {pos[0], pos[1], pos[2]}, {look[0], look[1], look[2]});
     const Emitters em = collect_emitters(s);
@@ -671,15 +673,17 @@ uint64_t orc_render_pt(void *h, uint64_t w, uint64_t hh, uint64_t fov, const flo
             const uint64_t pixel = py * w + px;
             const Ray prim = primary(c, px, py);
             V3 sum{0.f, 0.f, 0.f};
+            const uint64_t o = (py - row0) * w + px;
+            double *acc = out_sum64 ? out_sum64 + 3 * o : nullptr;
             for (uint32_t k = 0; k < spp; k++) {
-                pray_pcg32 g = pray_pcg32_stream(seed, pixel, k);
+                pray_pcg32 g = pray_pcg32_stream(seed, pixel, sample_offset + k);
                 const V3 L = mode == 0 ? path_kajiya(s, prim, b, max_depth, eps, g, segs)
                                        : path_nee(s, em, prim, b, max_depth, rr_depth, eps, g, segs);
                 sum = add(sum, L);
+                if (acc) acc[0] += (double)L.x, acc[1] += (double)L.y, acc[2] += (double)L.z;
             }
             const float ns = (float)spp;
             const V3 mean{sum.x / ns, sum.y / ns, sum.z / ns};
-            const uint64_t o = (py - row0) * w + px;
             if (out_rad) {
                 out_rad[3 * o] = mean.x;
                 out_rad[3 * o + 1] = mean.y;
