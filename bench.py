@@ -41,7 +41,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["icosphere", "soup"], default="icosphere")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--leaf-refine", type=int, default=4,
+    ap.add_argument("--leaf-refine", type=int, default=8,
                     help="device layout: sub-hierarchy inside reference leaves larger than this (0 = off)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     return ap.parse_args()

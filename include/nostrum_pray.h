@@ -53,7 +53,7 @@ typedef struct {
     float sah_intersection_cost;   /* triangleIntersectionCost (1.5) */
     int32_t build_threads;         /* host threads for the build, 0 = all */
     int32_t leaf_refine;           /* device layout only: leaves with more references than this get a
-                                      conservative sub-hierarchy (4; 0 = off). Results are unchanged. */
+                                      conservative sub-hierarchy (8; 0 = off). Results are unchanged. */
 } pray_tree_options;
 
 /* Ray-tracing frame parameters: the scene JSON's camera, lights and

@@ -341,7 +341,7 @@ void pray_tree_options_default(pray_tree_options *opt) {
     opt->sah_traversal_cost = 5.f;
     opt->sah_intersection_cost = 1.5f;
     opt->build_threads = 0;
-    opt->leaf_refine = 4;
+    opt->leaf_refine = 8;
 }
 
 pray_status pray_host_tree_build(const float *verts, uint64_t n, const pray_tree_options *opt,
