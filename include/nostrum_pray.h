@@ -195,6 +195,23 @@ pray_status pray_render_pt_host(pray_scene *s, const pray_pt_params *p, uint8_t 
 pray_status pray_accumulate_pt(pray_scene *s, const pray_pt_params *p, double *sum_dev,
                                unsigned long long *counters_dev, void *stream);
 
+/* Allocation-free path tracing (no counterpart in the reference). For host
+ * applications that must not have this library allocate device memory during
+ * a frame: engines that reserve all GPU memory up front for their own pool
+ * allocator, and frame loops that cannot afford cudaMalloc/cudaFree's
+ * implicit device synchronisation. Same frame as pray_render_pt with
+ * PRAY_SCHED_WAVEFRONT (PRAY_PT_NEE only; p->scheduler is ignored), but the
+ * path pool lives in a fixed 160 MiB static device array that every GPU
+ * loading this library holds until exit; frames above 1,103,744 pixels are
+ * rejected with PRAY_ERR_INVALID_ARGUMENT. Calls no cudaMalloc/cudaFree. The
+ * first call on each device looks up the array's address (and may load the
+ * module): make it before any stream capture. All calls share the array, so
+ * calls that overlap on the GPU race; order them (one stream, or events).
+ * rgb_dev / radiance_dev / counters_dev as for pray_render_pt (at least one
+ * of rgb_dev, radiance_dev). */
+pray_status pray_render_pt_noalloc(pray_scene *s, const pray_pt_params *p, uint8_t *rgb_dev, float *radiance_dev,
+                                   unsigned long long *counters_dev, void *stream);
+
 /* Relative mean squared error of an image against a reference, reduced in
  * FP64 on the device: mean over pixels and channels of
  * (x - r)^2 / (r^2 + 0.01), with x = img_scale * img[i], r = ref_scale * ref[i]

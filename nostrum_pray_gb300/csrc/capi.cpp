@@ -641,6 +641,28 @@ pray_status pray_accumulate_pt(pray_scene *s, const pray_pt_params *p, double *s
     return run_pt(s, L, p->scheduler, p->wavefront_paths, (cudaStream_t)stream);
 }
 
+pray_status pray_render_pt_noalloc(pray_scene *s, const pray_pt_params *p, uint8_t *rgb, float *radiance,
+                                   unsigned long long *counters, void *stream) {
+    if (!s || (!rgb && !radiance)) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    pray_status st = check_pt_params(p);
+    if (st != PRAY_OK) return st;
+    if (p->mode != PRAY_PT_NEE)
+        return set_error(PRAY_ERR_UNSUPPORTED, "the allocation-free path tracer runs PRAY_PT_NEE only");
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    PtLaunch L = make_pt_launch(p);
+    L.rgb = rgb;
+    L.radiance = radiance;
+    L.counters = counters;
+    std::string why;
+    e = launch_wavefront_noalloc(s->view(), L, p->wavefront_paths, (cudaStream_t)stream, why);
+    if (e != cudaSuccess) {
+        if (!why.empty()) return set_error(e == cudaErrorInvalidValue ? PRAY_ERR_INVALID_ARGUMENT : PRAY_ERR_CUDA, why);
+        return cuda_error(e, "allocation-free render_pt");
+    }
+    return PRAY_OK;
+}
+
 pray_status pray_relmse(const double *img, double img_scale, const double *ref, double ref_scale, uint64_t n,
                         double *out, void *stream) {
     if (!img || !ref || !out) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");

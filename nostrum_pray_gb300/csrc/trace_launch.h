@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
 
 #include <cuda_runtime.h>
 
@@ -66,6 +67,13 @@ WavefrontScratch wavefront_carve(void *base, uint64_t capacity, uint64_t pixels)
 // Enqueues one whole frame (all rounds) on `stream`; capturable in a graph.
 cudaError_t record_wavefront_frame(const DevScene &s, const PtLaunch &L, const WavefrontScratch &w, int sm_count,
                                    cudaStream_t stream);
+
+// Allocation-free wavefront frame on the static scratch of
+// wavefront_noalloc.cu (why receives a message on a size or set-up error).
+cudaError_t launch_wavefront_noalloc(const DevScene &s, const PtLaunch &L, uint64_t max_paths, cudaStream_t stream,
+                                     std::string &why);
+// Largest frame (pixels) the allocation-free path accepts.
+uint64_t noalloc_max_pixels();
 
 cudaError_t launch_relmse(const double *img, double img_scale, const double *ref, double ref_scale, uint64_t n,
                           double *out, cudaStream_t stream);

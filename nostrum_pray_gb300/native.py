@@ -65,7 +65,7 @@ EXPORTED = [
     "pray_host_tree_device_layout",
     "pray_camera", "pray_scene_create", "pray_scene_destroy", "pray_scene_stats", "pray_trace_closest",
     "pray_render_rt", "pray_render_rt_host", "pray_render_rt_counts", "pray_render_pt", "pray_render_pt_host",
-    "pray_accumulate_pt", "pray_relmse",
+    "pray_accumulate_pt", "pray_relmse", "pray_render_pt_noalloc",
 ]
 
 
@@ -96,6 +96,7 @@ def lib():
         L.pray_render_pt.argtypes = [_vp, ctypes.POINTER(PtParams), _vp, _vp, _vp, _vp]
         L.pray_render_pt_host.argtypes = [_vp, ctypes.POINTER(PtParams), _vp, _vp, _vp]
         L.pray_accumulate_pt.argtypes = [_vp, ctypes.POINTER(PtParams), _vp, _vp, _vp]
+        L.pray_render_pt_noalloc.argtypes = [_vp, ctypes.POINTER(PtParams), _vp, _vp, _vp, _vp]
         L.pray_relmse.argtypes = [_vp, ctypes.c_double, _vp, ctypes.c_double, _u64, _vp, _vp]
         for name in EXPORTED:
             if not hasattr(L, name):
@@ -252,6 +253,12 @@ class Scene:
         check(lib().pray_render_rt(self._h, ctypes.byref(p), _ptr(rgb), _ptr(ids), _ptr(ts), _ptr(counters),
                                    _stream(stream)))
         del keep
+
+    def render_pt_noalloc(self, params: PtParams, rgb=None, radiance=None, counters=None, stream=None) -> None:
+        """Allocation-free wavefront frame (static device scratch; see
+        pray_render_pt_noalloc in include/nostrum_pray.h)."""
+        check(lib().pray_render_pt_noalloc(self._h, ctypes.byref(params), _ptr(rgb), _ptr(radiance), _ptr(counters),
+                                           _stream(stream)))
 
     def accumulate_pt(self, params: PtParams, sum64, counters=None, stream=None) -> None:
         check(lib().pray_accumulate_pt(self._h, ctypes.byref(params), _ptr(sum64), _ptr(counters), _stream(stream)))
