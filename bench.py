@@ -39,7 +39,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["icosphere", "soup"], default="icosphere")
+    ap.add_argument("--workload", choices=["icosphere", "soup", "room", "batch"], default="icosphere")
+    ap.add_argument("--scheduler", choices=["pixel", "wavefront"], default="wavefront",
+                    help="room workload: path-tracing scheduler")
+    ap.add_argument("--spp", type=int, default=0, help="room/batch: samples per pixel (0 = workload default)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--leaf-refine", type=int, default=8,
                     help="device layout: sub-hierarchy inside reference leaves larger than this (0 = off)")
@@ -310,10 +313,100 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def _timed_frames(fn, steps, warmup, flush):
+    """CUDA-event time of `steps` calls of fn (L2 flushed before each)."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for k in range(steps):
+        flush.zero_()
+        starts[k].record(stream)
+        fn()
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in zip(starts, ends))
+
+
+def run_pt(args):
+    """Path tracing of the closed room (next-event estimation + Russian
+    roulette after depth 3), 1024x1024, 64 spp, depth 8."""
+    import torch
+    from nostrum_pray_gb300 import native, scenes
+    torch.cuda.set_device(0)
+    mesh = scenes.room()
+    spp = args.spp or 64
+    st = scenes.room_setup(1024, 1024, spp=spp, max_depth=8)
+    sc = native.Scene.from_setup(mesh, st, leaf_refine=args.leaf_refine)
+    sched = native.SCHED_WAVEFRONT if args.scheduler == "wavefront" else native.SCHED_PIXEL
+    p = native.pt_params(st, seed=1, mode=native.PT_NEE, rr_depth=3, scheduler=sched)
+    rgb = torch.empty((st.height, st.width, 3), dtype=torch.uint8, device="cuda")
+    cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    sc.render_pt(p, rgb, counters=cnt)
+    torch.cuda.synchronize()
+    paths, segs = int(cnt[0]), int(cnt[1])
+    ms = _timed_frames(lambda: sc.render_pt(p, rgb), args.steps, args.warmup, flush)
+    sec = ms / 1e3
+    line = {"metric": "Msamples/s", "value": round(paths * args.steps / sec / 1e6, 2), "unit": "Msamples/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"closed room {mesh.n} triangles, 1024x1024, {spp} spp, depth 8, NEE + "
+                                   f"Russian roulette after depth 3, {args.scheduler} scheduler",
+                       "l2": "flushed between steps"},
+            "mrays_per_s": round(segs * args.steps / sec / 1e6, 2), "segments_per_frame": segs}
+    print(json.dumps(line), flush=True)
+
+
+def run_batch(args):
+    """64 scenes (displaced icospheres and soups, lognormal triangle counts,
+    256^2..1024^2, 16 spp, depth 6) in one persistent launch, tuned first."""
+    import torch
+    from nostrum_pray_gb300 import native, scenes
+    torch.cuda.set_device(0)
+    spp = args.spp or 16
+    items = scenes.batch_workload(64, seed=0, spp=spp)
+    t0 = time.perf_counter()
+    scs, params, outs = [], [], []
+    for i, (mesh, st) in enumerate(items):
+        scs.append(native.Scene.from_setup(mesh, st, leaf_refine=args.leaf_refine))
+        params.append(native.pt_params(st, seed=i, mode=native.PT_KAJIYA))
+        outs.append((torch.empty((st.height, st.width, 3), dtype=torch.uint8, device="cuda"), None))
+    build_s = time.perf_counter() - t0
+    b = native.Batch(scs, params, outs)
+    t0 = time.perf_counter()
+    cfg, tune_ms = b.tune()
+    tune_s = time.perf_counter() - t0
+    cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+    b.render(cnt)
+    torch.cuda.synchronize()
+    paths, segs = int(cnt[0]), int(cnt[1])
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    ms = _timed_frames(lambda: b.render(), args.steps, args.warmup, flush)
+    sec = ms / 1e3
+    line = {"metric": "Msamples/s", "value": round(paths * args.steps / sec / 1e6, 2), "unit": "Msamples/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"64 scenes, {sum(m.n for m, _ in items)} triangles, "
+                                   f"{sum(st.width * st.height for _, st in items)} pixels, {spp} spp, depth 6, "
+                                   "one persistent graph-captured launch", "tuned": cfg.as_dict(),
+                       "tuning_s": round(tune_s, 2), "scene_build_s": round(build_s, 2),
+                       "l2": "flushed between steps"},
+            "mrays_per_s": round(segs * args.steps / sec / 1e6, 2), "segments_per_frame": segs}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "room":
+        run_pt(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_ours(args)
 

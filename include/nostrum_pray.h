@@ -212,6 +212,40 @@ pray_status pray_accumulate_pt(pray_scene *s, const pray_pt_params *p, double *s
 pray_status pray_render_pt_noalloc(pray_scene *s, const pray_pt_params *p, uint8_t *rgb_dev, float *radiance_dev,
                                    unsigned long long *counters_dev, void *stream);
 
+/* ---- batches: many scenes in one persistent launch (no reference counterpart) ---- */
+
+typedef struct pray_batch pray_batch;
+
+/* Launch shape of a batch: 32-pixel tiles (tile_w x tile_h == 32), threads
+ * per block, resident blocks per SM of the persistent grid (0 = as many as
+ * fit), traversal stack entries (32 or 64; 32 only when every scene's device
+ * hierarchy is shallower than 32). */
+typedef struct {
+    int32_t tile_w, tile_h;
+    int32_t block_threads;
+    int32_t blocks_per_sm;
+    int32_t stack_entries;
+} pray_batch_config;
+
+/* Records n scenes (all on one device) with one path-tracing frame each:
+ * params[i] as for pray_render_pt (scheduler and wavefront_paths ignored),
+ * rgb_dev[i] / radiance_dev[i] its outputs (device pointers; each may be
+ * NULL, not both). The scenes must outlive the batch. */
+pray_status pray_batch_create(pray_scene *const *scenes, const pray_pt_params *params, uint8_t *const *rgb_dev,
+                              float *const *radiance_dev, int32_t n, pray_batch **out);
+pray_status pray_batch_destroy(pray_batch *b);
+pray_status pray_batch_set_config(pray_batch *b, const pray_batch_config *cfg);
+/* Autotuner: times every candidate launch shape on the batch with one sample
+ * per pixel, keeps the fastest and returns it (best_ms: its time). Writes the
+ * outputs (with the one-sample frames). Synchronises. */
+pray_status pray_batch_tune(pray_batch *b, pray_batch_config *chosen, float *best_ms);
+/* Renders every scene's frame in one persistent launch (a memset and the
+ * kernel, captured once into a CUDA graph per launch shape) ordered after
+ * `stream`'s earlier work and before its later work. counters_dev (may be
+ * NULL): [paths, segments] accumulated; it is part of the captured graph, so
+ * keep passing the same pointer (a different one re-captures). */
+pray_status pray_batch_render(pray_batch *b, unsigned long long *counters_dev, void *stream);
+
 /* Relative mean squared error of an image against a reference, reduced in
  * FP64 on the device: mean over pixels and channels of
  * (x - r)^2 / (r^2 + 0.01), with x = img_scale * img[i], r = ref_scale * ref[i]

@@ -14,6 +14,7 @@
 
 #include <cuda_runtime.h>
 
+#include "batch_launch.h"
 #include "capi_internal.h"
 #include "device_layout.h"
 #include "host/camera.h"
@@ -96,6 +97,7 @@ struct pray_scene {
     float emit_area = 0.f;
     uint32_t n_gnodes = 0;
     uint64_t refined_leaves = 0;
+    int device_depth = 0;  // deepest node of the device hierarchy
     float tol = 0.f;
     uint64_t device_bytes = 0;
     // wavefront path tracer: scratch (path pool, queues), private stream,
@@ -440,7 +442,8 @@ pray_status pray_scene_create(const float *verts, const float *colors, const uin
         DeviceImage img;
         flatten_for_device(s->tree, pre, opt->leaf_refine, img);
         std::string bad;
-        if (!validate_device_image(img, bad)) return set_error(PRAY_ERR_UNSUPPORTED, "device layout: " + bad);
+        if (!validate_device_image(img, bad, &s->device_depth))
+            return set_error(PRAY_ERR_UNSUPPORTED, "device layout: " + bad);
         gnodes.swap(img.nodes);
         gtris.swap(img.tris);
         s->refined_leaves = img.refined_leaves;
@@ -660,6 +663,255 @@ pray_status pray_render_pt_noalloc(pray_scene *s, const pray_pt_params *p, uint8
         if (!why.empty()) return set_error(e == cudaErrorInvalidValue ? PRAY_ERR_INVALID_ARGUMENT : PRAY_ERR_CUDA, why);
         return cuda_error(e, "allocation-free render_pt");
     }
+    return PRAY_OK;
+}
+
+}  // extern "C"
+
+struct pray_batch {
+    int device = 0;
+    std::vector<pray_scene *> scenes;
+    std::vector<BatchItem> items;  // host copy; first_tile follows the tile shape
+    BatchItem *d_items = nullptr;
+    unsigned long long *d_next = nullptr;
+    uint64_t total_tiles = 0;
+    int max_depth = 0;
+    int sm_count = 0;
+    pray_batch_config cfg{8, 4, 128, 0, 64};
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long *exec_counters = nullptr;
+    void release() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (stream) cudaStreamDestroy(stream);
+        if (ev_in) cudaEventDestroy(ev_in);
+        if (ev_out) cudaEventDestroy(ev_out);
+        cudaFree(d_items);
+        cudaFree(d_next);
+        exec = nullptr, stream = nullptr, ev_in = ev_out = nullptr, d_items = nullptr, d_next = nullptr;
+    }
+};
+
+namespace {
+
+bool valid_batch_config(const pray_batch *b, const pray_batch_config &c, std::string &why) {
+    if (c.tile_w < 1 || c.tile_h < 1 || c.tile_w * c.tile_h != 32) {
+        why = "tile_w * tile_h must be 32";
+        return false;
+    }
+    if (c.block_threads < 32 || c.block_threads > 1024 || c.block_threads % 32) {
+        why = "block_threads must be a multiple of 32 in [32, 1024]";
+        return false;
+    }
+    if (c.stack_entries != 32 && c.stack_entries != 64) {
+        why = "stack_entries must be 32 or 64";
+        return false;
+    }
+    if (c.stack_entries == 32 && b->max_depth >= 32) {
+        why = "a scene's device hierarchy is too deep for a 32-entry stack";
+        return false;
+    }
+    if (c.blocks_per_sm < 0) {
+        why = "blocks_per_sm must be >= 0";
+        return false;
+    }
+    return true;
+}
+
+// Tile numbering for the batch's tile shape, uploaded with the items.
+pray_status upload_batch(pray_batch *b) {
+    uint64_t t = 0;
+    for (BatchItem &it : b->items) {
+        it.first_tile = t;
+        const uint64_t tx = (it.L.cam.width + b->cfg.tile_w - 1) / b->cfg.tile_w;
+        const uint64_t ty = (it.L.cam.height + b->cfg.tile_h - 1) / b->cfg.tile_h;
+        t += tx * ty;
+    }
+    b->total_tiles = t;
+    cudaError_t e = cudaMemcpy(b->d_items, b->items.data(), b->items.size() * sizeof(BatchItem),
+                               cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? PRAY_OK : cuda_error(e, "batch upload");
+}
+
+int batch_blocks(pray_batch *b, const pray_batch_config &c) {
+    int per_sm = 0;
+    if (batch_max_blocks_per_sm(c.block_threads, c.stack_entries, &per_sm) != cudaSuccess || per_sm < 1) per_sm = 1;
+    if (c.blocks_per_sm > 0) per_sm = std::min(per_sm, c.blocks_per_sm);
+    return per_sm * std::max(1, b->sm_count);
+}
+
+BatchLaunch batch_view(const pray_batch *b, unsigned long long *counters) {
+    BatchLaunch B;
+    B.items = b->d_items;
+    B.n_items = (int)b->items.size();
+    B.total_tiles = b->total_tiles;
+    B.next_tile = b->d_next;
+    B.tile_w = (uint32_t)b->cfg.tile_w;
+    B.tile_h = (uint32_t)b->cfg.tile_h;
+    B.counters = counters;
+    return B;
+}
+
+}  // namespace
+
+extern "C" {
+
+pray_status pray_batch_create(pray_scene *const *scenes, const pray_pt_params *params, uint8_t *const *rgb,
+                              float *const *radiance, int32_t n, pray_batch **out) {
+    if (!scenes || !params || !out || n <= 0) return set_error(PRAY_ERR_INVALID_ARGUMENT, "empty or NULL batch");
+    *out = nullptr;
+    auto b = std::make_unique<pray_batch>();
+    b->device = scenes[0] ? scenes[0]->device : 0;
+    for (int i = 0; i < n; i++) {
+        pray_scene *s = scenes[i];
+        if (!s) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL scene in batch");
+        if (s->device != b->device) return set_error(PRAY_ERR_INVALID_ARGUMENT, "batch scenes on different devices");
+        pray_pt_params p = params[i];
+        p.scheduler = PRAY_SCHED_PIXEL;
+        pray_status st = check_pt_params(&p);
+        if (st != PRAY_OK) return st;
+        uint8_t *o8 = rgb ? rgb[i] : nullptr;
+        float *of = radiance ? radiance[i] : nullptr;
+        if (!o8 && !of) return set_error(PRAY_ERR_INVALID_ARGUMENT, "batch item without an output");
+        BatchItem it;
+        std::memset(&it, 0, sizeof(it));
+        it.s = s->view();
+        it.L = make_pt_launch(&p);
+        it.L.rgb = o8;
+        it.L.radiance = of;
+        b->items.push_back(it);
+        b->scenes.push_back(s);
+        b->max_depth = std::max(b->max_depth, s->device_depth);
+    }
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->device);
+    if (b->max_depth >= 32) b->cfg.stack_entries = 64;
+    if ((e = cudaMalloc(&b->d_items, b->items.size() * sizeof(BatchItem))) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_next, sizeof(unsigned long long))) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming)) != cudaSuccess) {
+        b->release();
+        return cuda_error(e, "batch set-up");
+    }
+    pray_status st = upload_batch(b.get());
+    if (st != PRAY_OK) {
+        b->release();
+        return st;
+    }
+    *out = b.release();
+    return PRAY_OK;
+}
+
+pray_status pray_batch_destroy(pray_batch *b) {
+    if (!b) return PRAY_OK;
+    cudaSetDevice(b->device);
+    b->release();
+    delete b;
+    return PRAY_OK;
+}
+
+pray_status pray_batch_set_config(pray_batch *b, const pray_batch_config *cfg) {
+    if (!b || !cfg) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::string why;
+    if (!valid_batch_config(b, *cfg, why)) return set_error(PRAY_ERR_INVALID_ARGUMENT, why);
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    if ((e = cudaStreamSynchronize(b->stream)) != cudaSuccess) return cuda_error(e, "batch sync");
+    b->cfg = *cfg;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+    return upload_batch(b);
+}
+
+pray_status pray_batch_tune(pray_batch *b, pray_batch_config *chosen, float *best_ms) {
+    if (!b) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    const std::vector<BatchItem> full = b->items;
+    for (BatchItem &it : b->items) it.L.num_samples = 1;  // one sample per pixel while timing
+    static const int tiles[][2] = {{8, 4}, {4, 8}, {16, 2}, {32, 1}};
+    static const int threads[] = {64, 128, 256};
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    float best = -1.f;
+    pray_batch_config best_cfg = b->cfg;
+    pray_status st = PRAY_OK;
+    for (int stack : {32, 64}) {
+        if (stack == 32 && b->max_depth >= 32) continue;
+        for (const auto &tl : tiles)
+            for (int bt : threads)
+                for (int occ : {0, 2}) {
+                    pray_batch_config c{tl[0], tl[1], bt, occ, stack};
+                    b->cfg = c;
+                    if ((st = upload_batch(b)) != PRAY_OK) goto done;
+                    const int blocks = batch_blocks(b, c);
+                    const BatchLaunch B = batch_view(b, nullptr);
+                    // one untimed run (warms caches and loads the kernel), one timed
+                    if ((e = launch_batch_pt(B, bt, blocks, stack, b->stream)) != cudaSuccess ||
+                        (e = cudaEventRecord(t0, b->stream)) != cudaSuccess ||
+                        (e = launch_batch_pt(B, bt, blocks, stack, b->stream)) != cudaSuccess ||
+                        (e = cudaEventRecord(t1, b->stream)) != cudaSuccess ||
+                        (e = cudaEventSynchronize(t1)) != cudaSuccess) {
+                        st = cuda_error(e, "batch tuning run");
+                        goto done;
+                    }
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, t0, t1);
+                    if (best < 0.f || ms < best) best = ms, best_cfg = c;
+                }
+    }
+done:
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    b->items = full;
+    b->cfg = best_cfg;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+    pray_status up = upload_batch(b);
+    if (st != PRAY_OK) return st;
+    if (up != PRAY_OK) return up;
+    if (chosen) *chosen = best_cfg;
+    if (best_ms) *best_ms = best;
+    return PRAY_OK;
+}
+
+pray_status pray_batch_render(pray_batch *b, unsigned long long *counters, void *stream) {
+    if (!b) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    if (!b->exec || b->exec_counters != counters) {
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+        cudaGraph_t g = nullptr;
+        if ((e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+            return cuda_error(e, "batch capture");
+        const cudaError_t le =
+            launch_batch_pt(batch_view(b, counters), b->cfg.block_threads, batch_blocks(b, b->cfg),
+                            b->cfg.stack_entries, b->stream);
+        e = cudaStreamEndCapture(b->stream, &g);
+        if (le != cudaSuccess || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return cuda_error(le != cudaSuccess ? le : e, "batch capture");
+        }
+        e = cudaGraphInstantiate(&b->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            b->exec = nullptr;
+            return cuda_error(e, "batch graph instantiate");
+        }
+        b->exec_counters = counters;
+    }
+    cudaStream_t cs = (cudaStream_t)stream;
+    if ((e = cudaEventRecord(b->ev_in, cs)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(b->stream, b->ev_in, 0)) != cudaSuccess ||
+        (e = cudaGraphLaunch(b->exec, b->stream)) != cudaSuccess ||
+        (e = cudaEventRecord(b->ev_out, b->stream)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(cs, b->ev_out, 0)) != cudaSuccess)
+        return cuda_error(e, "batch launch");
     return PRAY_OK;
 }
 

@@ -149,7 +149,8 @@ void flatten_for_device(const BuiltTree &t, const std::vector<TriPre> &pre, int 
     f.put(0, 0, 0);
 }
 
-bool validate_device_image(const DeviceImage &img, std::string &why) {
+bool validate_device_image(const DeviceImage &img, std::string &why, int *max_depth) {
+    int deepest = 0;
     const uint64_t nn = img.nodes.size(), nt = img.tris.size();
     if (nn < 2) {
         why = "device image has no root";
@@ -167,6 +168,7 @@ bool validate_device_image(const DeviceImage &img, std::string &why) {
             why = "device hierarchy deeper than the traversal stack";
             return false;
         }
+        deepest = std::max(deepest, d);
         const GNode &g = img.nodes[i];
         if (g.b & kLeafFlag) {
             const uint64_t cnt = g.b & ~kLeafFlag;
@@ -189,6 +191,7 @@ bool validate_device_image(const DeviceImage &img, std::string &why) {
             todo.push_back({c, d + 1});
         }
     }
+    if (max_depth) *max_depth = deepest;
     return true;
 }
 

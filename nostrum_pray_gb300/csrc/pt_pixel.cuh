@@ -1,0 +1,202 @@
+// Per-pixel path tracing shared by the per-pixel kernel (pt.cu) and the
+// batched persistent kernel (batch.cu): one lane per pixel, the pixel's
+// samples in order, each an iterative bounce loop; all lanes of a warp call
+// pt_pixel together (the traversals are warp-collective).
+//
+// Mode 0 restates the reference's Kajiya path tracer
+// (evaluatePathRecursive, src/pray.cpp:342-364; evaluatePath,
+// src/pray.cpp:366-378): a miss returns the background, an emitter returns its
+// colour, a hit at depth >= max_depth returns black, otherwise one cosine
+// bounce whose result is multiplied by the albedo. The recursion multiplies
+// the deepest value first, so the albedos of a path are kept on a small
+// per-lane stack and applied in that order. Random numbers come from one
+// PCG32 stream per (seed, pixel, sample) (include/nostrum_pray_sampling.h).
+//
+// Mode 1 (no reference counterpart) adds next-event estimation to the
+// emitting triangles (area-weighted choice, uniform point, one occlusion ray)
+// and Russian roulette from rr_depth; emitters seen by a bounce ray end the
+// path without adding their emission (next-event estimation accounts for it).
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+
+#include "../../include/nostrum_pray_sampling.h"
+#include "device_layout.h"
+#include "trace_launch.h"
+#include "traverse.cuh"
+
+namespace pray_gpu {
+namespace dev {
+
+constexpr float kInvPi = 0.318309886183790671538f;
+constexpr float kShadowShrink = 0.999f;  // next-event occlusion ends short of the light point
+
+__device__ __forceinline__ float4 shade_n(const DevScene &s, int id) {
+    return __ldg(reinterpret_cast<const float4 *>(s.shade[id].n));
+}
+__device__ __forceinline__ float4 shade_c(const DevScene &s, int id) {
+    return __ldg(reinterpret_cast<const float4 *>(s.shade[id].c));
+}
+
+// Emitter index for a uniform u: first j with cdf[j] > u * total.
+__device__ __forceinline__ uint32_t pick_emitter(const DevScene &s, float u) {
+    const float target = u * s.emit_area;
+    uint32_t lo = 0, hi = s.n_emit - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(s.emit_cdf + mid) > target) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+// Every lane of a warp runs the same sample loop and bounce iterations (a
+// finished path idles until the warp's last path ends) so that the
+// warp-collective traversals line up.
+template <int kStackN>
+__device__ __forceinline__ void pt_pixel(const DevScene &s, const PtLaunch &L, bool active, uint32_t px,
+                                         uint32_t py, uint32_t &segments) {
+    constexpr unsigned kFull = 0xFFFFFFFFu;
+    const uint64_t pixel = active ? (uint64_t)py * L.cam.width + px : 0;
+    const RayF prim = primary_ray(L.cam, active ? px : 0, active ? py : 0);
+    float sr = 0.f, sg = 0.f, sb = 0.f;
+    float alb_r[kMaxPtDepth], alb_g[kMaxPtDepth], alb_b[kMaxPtDepth];
+    double ax = 0, ay = 0, az = 0;
+    if (active && L.sum64) ax = L.sum64[3 * pixel], ay = L.sum64[3 * pixel + 1], az = L.sum64[3 * pixel + 2];
+    const bool any_geometry = s.n_refs > 0;
+    for (uint32_t smp = 0; smp < L.num_samples; smp++) {
+        pray_pcg32 rng = pray_pcg32_stream(L.seed, pixel, L.sample_offset + smp);
+        RayF r = prim;
+        float lr = 0.f, lg = 0.f, lb = 0.f;
+        float tr = 1.f, tg = 1.f, tb = 1.f;
+        uint32_t depth = 0;
+        bool alive = active;
+        while (__any_sync(kFull, alive)) {
+            float t;
+            const int pos = traverse<false, false, kStackN>(s, r, L.eps, 0.f, alive && any_geometry, t);
+            // next-event occlusion job of this bounce (mode 1)
+            bool need = false;
+            RayF sray = r;
+            float sd2 = 0.f, cxr = 0.f, cxg = 0.f, cxb = 0.f;
+            float4 nrm = make_float4(0.f, 0.f, 0.f, 0.f), col = nrm;
+            float hx = 0.f, hy = 0.f, hz = 0.f;
+            if (alive) {
+                segments++;
+                if (pos < 0) {
+                    if (L.mode == 0) lr = L.bg[0], lg = L.bg[1], lb = L.bg[2];
+                    else lr = lr + tr * L.bg[0], lg = lg + tg * L.bg[1], lb = lb + tb * L.bg[2];
+                    alive = false;
+                } else {
+                    const int id = (int)__float_as_uint(__ldg(&s.tris[pos].v0[3]));
+                    nrm = shade_n(s, id), col = shade_c(s, id);
+                    if (nrm.w != 0.f) {
+                        if (L.mode == 0) lr = col.x, lg = col.y, lb = col.z;
+                        else if (depth == 0) lr = lr + tr * col.x, lg = lg + tg * col.y, lb = lb + tb * col.z;
+                        alive = false;
+                    } else if (depth >= L.max_depth) {
+                        if (L.mode == 0) lr = 0.f, lg = 0.f, lb = 0.f;
+                        alive = false;
+                    } else {
+                        hx = r.ox + r.dx * t, hy = r.oy + r.dy * t, hz = r.oz + r.dz * t;
+                        if (L.mode != 0 && s.n_emit > 0) {
+                            const float ue = pray_uniform(&rng), ua = pray_uniform(&rng), ub = pray_uniform(&rng);
+                            const GTri *E = s.emit_tris + pick_emitter(s, ue);
+                            const float4 ev0 = __ldg(reinterpret_cast<const float4 *>(E->v0));
+                            const float4 ee1 = __ldg(reinterpret_cast<const float4 *>(E->e1));
+                            const float4 ee2 = __ldg(reinterpret_cast<const float4 *>(E->e2));
+                            const float su = sqrtf(ua);
+                            const float b1 = su * (1.f - ub), b2 = su * ub;
+                            const float yx = ev0.x + ee1.x * b1 + ee2.x * b2;
+                            const float yy = ev0.y + ee1.y * b1 + ee2.y * b2;
+                            const float yz = ev0.z + ee1.z * b1 + ee2.z * b2;
+                            float wx = yx - hx, wy = yy - hy, wz = yz - hz;
+                            const float d2 = wx * wx + wy * wy + wz * wz;
+                            if (d2 > 0.f) {
+                                const float inv = 1.0f / sqrtf(d2);
+                                wx *= inv, wy *= inv, wz *= inv;
+                                const int eid = (int)__float_as_uint(ev0.w);
+                                const float4 en = shade_n(s, eid), ec = shade_c(s, eid);
+                                const float cx = nrm.x * wx + nrm.y * wy + nrm.z * wz;
+                                const float cy = -(en.x * wx + en.y * wy + en.z * wz);
+                                if (cx > 0.f && cy > 0.f) {
+                                    need = true;
+                                    sray = make_ray(hx, hy, hz, wx, wy, wz);
+                                    sd2 = d2 * kShadowShrink;
+                                    const float g = ((cx * cy) * s.emit_area) * kInvPi / d2;
+                                    cxr = ((tr * col.x) * ec.x) * g;
+                                    cxg = ((tg * col.y) * ec.y) * g;
+                                    cxb = ((tb * col.z) * ec.z) * g;
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+            float dummy;
+            const bool occluded = traverse<true, false, kStackN>(s, sray, L.eps, sd2, need, dummy) >= 0;
+            if (need) {
+                segments++;
+                if (!occluded) lr = lr + cxr, lg = lg + cxg, lb = lb + cxb;
+            }
+            if (alive) {
+                // cosine bounce (and, in mode 1, Russian roulette)
+                if (L.mode == 0) alb_r[depth] = col.x, alb_g[depth] = col.y, alb_b[depth] = col.z;
+                const float u1 = pray_uniform(&rng), u2 = pray_uniform(&rng);
+                const float n3[3] = {nrm.x, nrm.y, nrm.z};
+                float d[3];
+                pray_sample_hemisphere(n3, u1, u2, d);
+                r = make_ray(hx, hy, hz, d[0], d[1], d[2]);
+                if (L.mode != 0) {
+                    tr = tr * col.x, tg = tg * col.y, tb = tb * col.z;
+                    if (depth >= L.rr_depth) {
+                        const float q = smin(smax(smax(tr, tg), tb), 0.95f);
+                        if (!(pray_uniform(&rng) < q)) alive = false;
+                        else tr = tr / q, tg = tg / q, tb = tb / q;
+                    }
+                }
+                depth++;
+            }
+        }
+        if (active) {
+            if (L.mode == 0) {
+                while (depth > 0) {
+                    depth--;
+                    lr = lr * alb_r[depth], lg = lg * alb_g[depth], lb = lb * alb_b[depth];
+                }
+            }
+            sr = sr + lr, sg = sg + lg, sb = sb + lb;
+            if (L.sum64) ax = ax + (double)lr, ay = ay + (double)lg, az = az + (double)lb;
+        }
+    }
+    if (active) {
+        if (L.sum64) L.sum64[3 * pixel] = ax, L.sum64[3 * pixel + 1] = ay, L.sum64[3 * pixel + 2] = az;
+        const float ns = (float)L.num_samples;
+        const float mr = sr / ns, mg = sg / ns, mb = sb / ns;
+        if (L.radiance) {
+            float *o = L.radiance + 3 * pixel;
+            o[0] = mr, o[1] = mg, o[2] = mb;
+        }
+        if (L.rgb) {
+            uint8_t *o = L.rgb + 3 * pixel;
+            o[0] = (uint8_t)quantise(smax(0.f, smin(1.f, mr)));
+            o[1] = (uint8_t)quantise(smax(0.f, smin(1.f, mg)));
+            o[2] = (uint8_t)quantise(smax(0.f, smin(1.f, mb)));
+        }
+    }
+}
+
+// Warp-aggregated [paths, segments] into counters (all lanes call).
+__device__ __forceinline__ void count_paths(unsigned long long *counters, bool active, uint32_t num_samples,
+                                            uint32_t segments) {
+    constexpr unsigned kFull = 0xFFFFFFFFu;
+    const uint32_t paths = __popc(__ballot_sync(kFull, active)) * num_samples;
+    for (int o = 16; o > 0; o >>= 1) segments += __shfl_xor_sync(kFull, segments, o);
+    if ((threadIdx.x & 31) == 0 && counters) {
+        atomicAdd(counters + 0, (unsigned long long)paths);
+        atomicAdd(counters + 1, (unsigned long long)segments);
+    }
+}
+
+}  // namespace dev
+}  // namespace pray_gpu

@@ -124,9 +124,10 @@ __device__ __forceinline__ bool pop_node(const uint32_t *stk_a, const uint32_t *
 // record or -1, its distance in best_t.
 // Any hit (kAny = true): returns >= 0 once a triangle with t > 0 and
 // t * t < d2 is found (the occlusion test of src/pray.cpp:42).
-template <bool kAny, bool kCount = false>
+template <bool kAny, bool kCount = false, int kStackN = kStack>
 __device__ __forceinline__ int traverse(const DevScene &s, const RayF &r, float eps, float d2, bool valid,
                                         float &best_t, FetchCount *fc = nullptr) {
+    static_assert(kStackN >= 2 && kStackN <= kStack, "stack entries");
     constexpr unsigned kFull = 0xFFFFFFFFu;
     best_t = FLT_MAX;
     int best = -1;
@@ -146,8 +147,8 @@ __device__ __forceinline__ int traverse(const DevScene &s, const RayF &r, float 
             have_node = true;
         }
     }
-    uint32_t stk_a[kStack], stk_b[kStack];
-    float stk_t[kStack];
+    uint32_t stk_a[kStackN], stk_b[kStackN];
+    float stk_t[kStackN];
     int sp = 0;
     while (__any_sync(kFull, have_node || have_leaf)) {
         // 1. interior nodes, until every lane has found a leaf

@@ -52,6 +52,14 @@ class PtParams(ctypes.Structure):
                 ("wavefront_paths", ctypes.c_uint32)]
 
 
+class BatchConfig(ctypes.Structure):
+    _fields_ = [("tile_w", _i32), ("tile_h", _i32), ("block_threads", _i32), ("blocks_per_sm", _i32),
+                ("stack_entries", _i32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class PrayError(RuntimeError):
     pass
 
@@ -66,6 +74,7 @@ EXPORTED = [
     "pray_camera", "pray_scene_create", "pray_scene_destroy", "pray_scene_stats", "pray_trace_closest",
     "pray_render_rt", "pray_render_rt_host", "pray_render_rt_counts", "pray_render_pt", "pray_render_pt_host",
     "pray_accumulate_pt", "pray_relmse", "pray_render_pt_noalloc",
+    "pray_batch_create", "pray_batch_destroy", "pray_batch_set_config", "pray_batch_tune", "pray_batch_render",
 ]
 
 
@@ -97,6 +106,11 @@ def lib():
         L.pray_render_pt_host.argtypes = [_vp, ctypes.POINTER(PtParams), _vp, _vp, _vp]
         L.pray_accumulate_pt.argtypes = [_vp, ctypes.POINTER(PtParams), _vp, _vp, _vp]
         L.pray_render_pt_noalloc.argtypes = [_vp, ctypes.POINTER(PtParams), _vp, _vp, _vp, _vp]
+        L.pray_batch_create.argtypes = [_vp, ctypes.POINTER(PtParams), _vp, _vp, _i32, ctypes.POINTER(_vp)]
+        L.pray_batch_destroy.argtypes = [_vp]
+        L.pray_batch_set_config.argtypes = [_vp, ctypes.POINTER(BatchConfig)]
+        L.pray_batch_tune.argtypes = [_vp, ctypes.POINTER(BatchConfig), ctypes.POINTER(_f32)]
+        L.pray_batch_render.argtypes = [_vp, _vp, _vp]
         L.pray_relmse.argtypes = [_vp, ctypes.c_double, _vp, ctypes.c_double, _u64, _vp, _vp]
         for name in EXPORTED:
             if not hasattr(L, name):
@@ -306,3 +320,40 @@ def _stream(stream) -> Optional[int]:
             pass
         return None
     return getattr(stream, "cuda_stream", stream)
+
+
+class Batch:
+    """Many scenes, one path-traced frame each, rendered by one persistent
+    launch (pray_batch_*). outputs: per scene an (rgb, radiance) pair of torch
+    CUDA tensors (either may be None)."""
+
+    def __init__(self, scenes, params, outputs):
+        n = len(scenes)
+        handles = (_vp * n)(*[sc._h.value for sc in scenes])
+        ps = (PtParams * n)(*params)
+        rgbs = (_vp * n)(*[_ptr(o[0]) for o in outputs])
+        rads = (_vp * n)(*[_ptr(o[1]) for o in outputs])
+        h = _vp()
+        check(lib().pray_batch_create(handles, ps, rgbs, rads, n, ctypes.byref(h)))
+        self._h = h
+        self._keep = (scenes, outputs)
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.pray_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_config(self, cfg: BatchConfig) -> None:
+        check(lib().pray_batch_set_config(self._h, ctypes.byref(cfg)))
+
+    def tune(self):
+        cfg = BatchConfig()
+        ms = _f32()
+        check(lib().pray_batch_tune(self._h, ctypes.byref(cfg), ctypes.byref(ms)))
+        return cfg, ms.value
+
+    def render(self, counters=None, stream=None) -> None:
+        check(lib().pray_batch_render(self._h, _ptr(counters), _stream(stream)))

@@ -330,3 +330,36 @@ def random_room(seed: int, grid: int = 16) -> Mesh:
         boxes.append((c, s, float(rng.uniform(-45, 45)), tuple(rng.uniform(0.1, 0.9, 3))))
     return room(grid=grid, boxes=boxes, wall_albedo=tuple(rng.uniform(0.1, 0.9, 3)),
                 light_size=float(rng.uniform(0.3, 0.8)))
+
+
+# --------------------------------------------------------------------------
+# Batched workload: n independent scenes, each a displaced icosphere or a
+# triangle soup with a lognormal triangle count (median 40k, clipped to
+# [1k, 500k], sigma 1), a square resolution from {256, 512, 768, 1024}, a
+# random camera on a sphere of radius 3 looking at the origin, a sky
+# background, 16 spp, depth 6, SAH trees.
+
+def batch_workload(n: int = 64, seed: int = 0, median: int = 40_000, sigma: float = 1.0, lo: int = 1_000,
+                   hi: int = 500_000, spp: int = 16, depth: int = 6, resolutions=(256, 512, 768, 1024)):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        count = int(np.clip(np.exp(rng.normal(np.log(median), sigma)), lo, hi))
+        sphere = bool(rng.random() < 0.5)
+        res = int(resolutions[int(rng.integers(len(resolutions)))])
+        az, el = rng.uniform(0, 2 * np.pi), rng.uniform(-1.0, 1.0)
+        pos = 3.0 * np.array([np.cos(el) * np.cos(az), np.sin(el), np.cos(el) * np.sin(az)])
+        albedo = tuple(float(x) for x in rng.uniform(0.3, 0.9, 3))
+        if sphere:
+            level = int(np.clip(round(np.log(count / 20.0) / np.log(4.0)), 2, 7))
+            mesh = icosphere(level, seed=seed * 1000 + i, albedo=albedo)
+        else:
+            mesh = soup(count, seed * 1000 + i)
+            mesh.verts = (mesh.verts * 2.0 - 1.0).astype(np.float32)
+            mesh.colors[:] = np.asarray(albedo, np.float32)
+        setup = RenderSetup(width=res, height=res, fov=45, cam_pos=tuple(float(x) for x in pos),
+                            cam_look=tuple(float(x) for x in -pos), lights=[], background=(0.7, 0.8, 1.0),
+                            tree="sah", leaf_size=32, max_depth=20, sah_ct=1.0, sah_ci=1.5, det_eps=0.0,
+                            method="path_tracing", max_depth_pt=depth, num_samples=spp)
+        out.append((mesh, setup))
+    return out
