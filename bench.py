@@ -39,7 +39,12 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["icosphere", "soup", "room", "batch"], default="icosphere")
+    ap.add_argument("--workload", choices=["icosphere", "soup", "room", "batch", "denoise"], default="icosphere")
+    ap.add_argument("--dn-steps", type=int, default=1000, help="denoise: training steps")
+    ap.add_argument("--dn-train", type=int, default=96, help="denoise: training rooms")
+    ap.add_argument("--dn-eval", type=int, default=16, help="denoise: held-out rooms")
+    ap.add_argument("--dn-res", type=int, default=128, help="denoise: image size")
+    ap.add_argument("--dn-ref-spp", type=int, default=1024, help="denoise: reference samples per pixel")
     ap.add_argument("--scheduler", choices=["pixel", "wavefront"], default="wavefront",
                     help="room workload: path-tracing scheduler")
     ap.add_argument("--spp", type=int, default=0, help="room/batch: samples per pixel (0 = workload default)")
@@ -399,6 +404,51 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def run_denoise(args):
+    """Learned denoiser: train on rooms rendered by the path tracer, then time
+    to relMSE <= 0.01 against FP64-accumulated references, denoised vs plain."""
+    import torch
+    from nostrum_pray_gb300 import denoise as D, native
+    torch.cuda.set_device(0)
+    cfg = D.DenoiseConfig(res=args.dn_res, spp_ref=args.dn_ref_spp, train_rooms=args.dn_train,
+                          eval_rooms=args.dn_eval, steps=args.dn_steps)
+    t0 = time.perf_counter()
+    train_seeds = list(range(cfg.seed, cfg.seed + cfg.train_rooms))
+    eval_seeds = list(range(cfg.seed + 100_000, cfg.seed + 100_000 + cfg.eval_rooms))
+    _, rad, feat, ref = D.make_dataset(cfg, train_seeds, torch)
+    eval_scs, _, _, eval_refs = D.make_dataset(cfg, eval_seeds, torch)
+    data_s = time.perf_counter() - t0
+    den = native.Denoiser(seed=cfg.seed)
+    t0 = time.perf_counter()
+    losses = D.train(den, rad, feat, ref, cfg, torch)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    # calibration of the fallback sample count on a few training rooms
+    calib = [D.plain_curve(cfg, sc, ref[i], train_seeds[i], torch) for i, sc in enumerate(D.make_dataset(
+        cfg, train_seeds[:4], torch)[0])]
+    fb_spp = D.fallback_spp_from(calib, cfg.target)
+    res = D.evaluate(cfg, den, {s: (sc, eval_refs[i]) for i, (s, sc) in enumerate(zip(eval_seeds, eval_scs))},
+                     torch, fb_spp)
+    rows = res["rooms"]
+    tp = [r["time_plain_s"] for r in rows if r["spp_plain_to_target"] is not None]
+    td = [r["time_final_s"] for r in rows]
+    ok_d = sum(1 for r in rows if r["relmse_final"] <= cfg.target)
+    line = {"metric": "time to relMSE<=0.01, denoised / plain", "value": round(float(np.mean(td) / np.mean(tp)), 4)
+            if tp else None, "unit": "ratio", "n_gpus": 1, "higher_is_better": False, "dtype": "bf16",
+            "data": "synthetic", "config": {"workload": f"procedural rooms {cfg.res}x{cfg.res}, {cfg.spp_in} spp input,"
+                                                        f" {cfg.spp_ref} spp FP64 reference, {cfg.train_rooms} train /"
+                                                        f" {cfg.eval_rooms} held-out rooms, {cfg.steps} Adam steps"},
+            "relmse_noisy_mean": float(np.mean([r["relmse_noisy"] for r in rows])),
+            "relmse_denoised_mean": float(np.mean([r["relmse_denoised"] for r in rows])),
+            "relmse_final_mean": float(np.mean([r["relmse_final"] for r in rows])),
+            "rooms_meeting_target": ok_d, "fallbacks": sum(r["fallback"] for r in rows), "fallback_spp": fb_spp,
+            "time_plain_mean_s": float(np.mean(tp)) if tp else None, "time_denoised_mean_s": float(np.mean(td)),
+            "spp_plain_to_target": [r["spp_plain_to_target"] for r in rows],
+            "loss_first_last": [losses[0][1], losses[-1][1]], "data_s": round(data_s, 1),
+            "train_s": round(train_s, 1)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -407,6 +457,8 @@ def main():
         run_pt(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "denoise":
+        run_denoise(args)
     else:
         run_ours(args)
 

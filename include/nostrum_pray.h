@@ -176,7 +176,8 @@ pray_status pray_render_rt_host(pray_scene *s, const pray_rt_params *p, uint8_t 
 pray_status pray_render_rt_counts(pray_scene *s, const pray_rt_params *p, uint64_t *out);
 
 /* One path-traced frame (pathTrace, src/pray.cpp:592-615) into device
- * memory: rgb_dev as for pray_render_rt; radiance_dev (may be NULL) receives
+ * memory: rgb_dev as for pray_render_rt (may be NULL when radiance_dev is
+ * given); radiance_dev (may be NULL) receives
  * the per-pixel mean radiance (height x width x 3 floats) before clamping;
  * counters_dev (may be NULL) is incremented by [paths, ray segments]. */
 pray_status pray_render_pt(pray_scene *s, const pray_pt_params *p, uint8_t *rgb_dev, float *radiance_dev,
@@ -245,6 +246,43 @@ pray_status pray_batch_tune(pray_batch *b, pray_batch_config *chosen, float *bes
  * NULL): [paths, segments] accumulated; it is part of the captured graph, so
  * keep passing the same pointer (a different one re-captures). */
 pray_status pray_batch_render(pray_batch *b, unsigned long long *counters_dev, void *stream);
+
+/* ---- learned denoiser (no reference counterpart) ---- */
+
+/* First-hit features for the denoiser (camera of p): per pixel albedo (or
+ * emitted colour) 3, geometric normal 3, hit distance 1 as FP16 bits,
+ * height x width x 7 (zeros on a miss). */
+pray_status pray_render_features(pray_scene *s, const pray_pt_params *p, uint16_t *features_dev, void *stream);
+
+typedef struct pray_denoiser pray_denoiser;
+
+/* Five-level convolutional U-Net (channels 32-48-64-96-128, two 3x3
+ * convolutions with ReLU per level, 2x2 average pooling, nearest 2x
+ * upsampling, concatenated skips, 3x3 output convolution), BF16 weights and
+ * activations, FP32 accumulation. Input per pixel: log(1 + noisy radiance),
+ * the 7 features; output: radiance. Weights He-initialised from seed.
+ * Parameter vector: per convolution in forward order, weights
+ * [cout][3][3][cin] then biases [cout]. */
+pray_status pray_denoiser_create(int32_t device, uint64_t seed, pray_denoiser **out);
+pray_status pray_denoiser_destroy(pray_denoiser *d);
+pray_status pray_denoiser_num_params(const pray_denoiser *d, uint64_t *n);
+pray_status pray_denoiser_get_params(const pray_denoiser *d, float *host);
+pray_status pray_denoiser_set_params(pray_denoiser *d, const float *host);
+/* Denoises n images of h x w (multiples of 16): radiance_dev n*h*w*3 floats,
+ * features_dev n*h*w*7 FP16, out_dev n*h*w*3 floats (device pointers). */
+pray_status pray_denoise(pray_denoiser *d, const float *radiance_dev, const uint16_t *features_dev, int32_t n,
+                         int32_t h, int32_t w, float *out_dev, void *stream);
+/* One Adam step (lr; betas 0.9 / 0.999) on the L1 loss between log(1 + output)
+ * and log(1 + target_dev). loss_host (may be NULL) receives the loss before
+ * the step (synchronises). */
+pray_status pray_denoiser_train_step(pray_denoiser *d, const float *radiance_dev, const uint16_t *features_dev,
+                                     const float *target_dev, int32_t n, int32_t h, int32_t w, float lr,
+                                     float *loss_host, void *stream);
+/* Loss and parameter gradients without an update (synchronises):
+ * grads_host has pray_denoiser_num_params floats. */
+pray_status pray_denoiser_gradients(pray_denoiser *d, const float *radiance_dev, const uint16_t *features_dev,
+                                    const float *target_dev, int32_t n, int32_t h, int32_t w, float *loss_host,
+                                    float *grads_host);
 
 /* Relative mean squared error of an image against a reference, reduced in
  * FP64 on the device: mean over pixels and channels of

@@ -16,6 +16,7 @@
 
 #include "batch_launch.h"
 #include "capi_internal.h"
+#include "denoise_net.h"
 #include "device_layout.h"
 #include "host/camera.h"
 #include "host/flatten.h"
@@ -619,7 +620,7 @@ pray_status pray_render_rt_counts(pray_scene *s, const pray_rt_params *p, uint64
 
 pray_status pray_render_pt(pray_scene *s, const pray_pt_params *p, uint8_t *rgb, float *radiance,
                            unsigned long long *counters, void *stream) {
-    if (!s || !rgb) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!s || (!rgb && !radiance)) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
     pray_status st = check_pt_params(p);
     if (st != PRAY_OK) return st;
     cudaError_t e = cudaSetDevice(s->device);
@@ -913,6 +914,118 @@ pray_status pray_batch_render(pray_batch *b, unsigned long long *counters, void 
         (e = cudaStreamWaitEvent(cs, b->ev_out, 0)) != cudaSuccess)
         return cuda_error(e, "batch launch");
     return PRAY_OK;
+}
+
+pray_status pray_render_features(pray_scene *s, const pray_pt_params *p, uint16_t *features, void *stream) {
+    if (!s || !p || !features) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (p->width == 0 || p->height == 0 || p->width > 65536 || p->height > 65536)
+        return set_error(PRAY_ERR_INVALID_ARGUMENT, "width and height must be in [1, 65536]");
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    const CameraConsts cam = make_camera(p->width, p->height, p->fov, p->camera_position, p->camera_look);
+    e = launch_features(s->view(), cam, p->det_epsilon, reinterpret_cast<__half *>(features), (cudaStream_t)stream);
+    return e == cudaSuccess ? PRAY_OK : cuda_error(e, "features launch");
+}
+
+}  // extern "C"
+
+struct pray_denoiser {
+    Denoiser net;
+};
+
+namespace {
+
+pray_status check_dims(int32_t n, int32_t h, int32_t w) {
+    if (n <= 0 || h <= 0 || w <= 0 || h % 16 || w % 16 || (int64_t)n * h * w > (1ll << 31) / 256)
+        return set_error(PRAY_ERR_INVALID_ARGUMENT, "images must be non-empty, h and w multiples of 16");
+    return PRAY_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+pray_status pray_denoiser_create(int32_t device, uint64_t seed, pray_denoiser **out) {
+    if (!out) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = nullptr;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    auto d = std::make_unique<pray_denoiser>();
+    d->net.device = device;
+    if ((e = d->net.init(seed)) != cudaSuccess) return cuda_error(e, "denoiser init");
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return cuda_error(e, "denoiser init");
+    *out = d.release();
+    return PRAY_OK;
+}
+
+pray_status pray_denoiser_destroy(pray_denoiser *d) {
+    if (!d) return PRAY_OK;
+    cudaSetDevice(d->net.device);
+    delete d;
+    return PRAY_OK;
+}
+
+pray_status pray_denoiser_num_params(const pray_denoiser *d, uint64_t *n) {
+    if (!d || !n) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    *n = d->net.num_params();
+    return PRAY_OK;
+}
+
+pray_status pray_denoiser_get_params(const pray_denoiser *d, float *host) {
+    if (!d || !host) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    cudaSetDevice(d->net.device);
+    cudaError_t e = d->net.get_params(host);
+    return e == cudaSuccess ? PRAY_OK : cuda_error(e, "denoiser get_params");
+}
+
+pray_status pray_denoiser_set_params(pray_denoiser *d, const float *host) {
+    if (!d || !host) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    cudaSetDevice(d->net.device);
+    cudaError_t e = d->net.set_params(host);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    return e == cudaSuccess ? PRAY_OK : cuda_error(e, "denoiser set_params");
+}
+
+pray_status pray_denoise(pray_denoiser *d, const float *rad, const uint16_t *feat, int32_t n, int32_t h, int32_t w,
+                         float *out, void *stream) {
+    if (!d || !rad || !feat || !out) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    pray_status st = check_dims(n, h, w);
+    if (st != PRAY_OK) return st;
+    cudaSetDevice(d->net.device);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = d->net.forward(rad, reinterpret_cast<const __half *>(feat), n, h, w, s);
+    if (e == cudaSuccess) e = d->net.output_radiance(out, s);
+    return e == cudaSuccess ? PRAY_OK : cuda_error(e, "denoise");
+}
+
+pray_status pray_denoiser_train_step(pray_denoiser *d, const float *rad, const uint16_t *feat, const float *target,
+                                     int32_t n, int32_t h, int32_t w, float lr, float *loss_host, void *stream) {
+    if (!d || !rad || !feat || !target) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    pray_status st = check_dims(n, h, w);
+    if (st != PRAY_OK) return st;
+    cudaSetDevice(d->net.device);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = d->net.forward(rad, reinterpret_cast<const __half *>(feat), n, h, w, s);
+    if (e == cudaSuccess) e = d->net.backward(target, s);
+    if (e == cudaSuccess && loss_host)
+        e = cudaMemcpyAsync(loss_host, d->net.loss_device(), 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = d->net.apply_adam(lr, s);
+    if (e == cudaSuccess && loss_host) e = cudaStreamSynchronize(s);
+    return e == cudaSuccess ? PRAY_OK : cuda_error(e, "denoiser train step");
+}
+
+pray_status pray_denoiser_gradients(pray_denoiser *d, const float *rad, const uint16_t *feat, const float *target,
+                                    int32_t n, int32_t h, int32_t w, float *loss_host, float *grads_host) {
+    if (!d || !rad || !feat || !target || !grads_host) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    pray_status st = check_dims(n, h, w);
+    if (st != PRAY_OK) return st;
+    cudaSetDevice(d->net.device);
+    cudaError_t e = d->net.forward(rad, reinterpret_cast<const __half *>(feat), n, h, w, 0);
+    if (e == cudaSuccess) e = d->net.backward(target, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess && loss_host) e = cudaMemcpy(loss_host, d->net.loss_device(), 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = d->net.get_grads(grads_host);
+    return e == cudaSuccess ? PRAY_OK : cuda_error(e, "denoiser gradients");
 }
 
 pray_status pray_relmse(const double *img, double img_scale, const double *ref, double ref_scale, uint64_t n,

@@ -1,0 +1,277 @@
+// The denoiser network on the device: a five-level convolutional U-Net
+// (channels 32-48-64-96-128, two 3x3 convolutions with ReLU per level, 2x2
+// average pooling down, nearest 2x upsampling up, skip connections by channel
+// concatenation, a final 3x3 convolution to RGB). Input per pixel:
+// log(1 + radiance) of the noisy render (3), first-hit albedo (3), normal (3)
+// and depth (1); output: log(1 + radiance) of the estimate. Trained with an L1
+// loss in that log space and Adam. Every kernel is in denoise_ops.cu.
+#include "denoise_net.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+
+namespace pray_gpu {
+
+namespace {
+
+// (cin, cout, relu) of the 19 convolutions in forward order
+const int kConvs[][3] = {
+    {10, 32, 1}, {32, 32, 1},     // e0
+    {32, 48, 1}, {48, 48, 1},     // e1
+    {48, 64, 1}, {64, 64, 1},     // e2
+    {64, 96, 1}, {96, 96, 1},     // e3
+    {96, 128, 1}, {128, 128, 1},  // e4 (bottleneck)
+    {224, 96, 1}, {96, 96, 1},    // d3: up(e4) 128 + e3 96
+    {160, 64, 1}, {64, 64, 1},    // d2: up(d3) 96 + e2 64
+    {112, 48, 1}, {48, 48, 1},    // d1: up(d2) 64 + e1 48
+    {80, 32, 1}, {32, 32, 1},     // d0: up(d1) 48 + e0 32
+    {32, 3, 0},                   // out
+};
+constexpr int kNumConvs = 19;
+const int kEnc[5] = {32, 48, 64, 96, 128};
+
+template <class T>
+cudaError_t dalloc(T *&p, size_t n) {
+    return cudaMalloc(reinterpret_cast<void **>(&p), std::max<size_t>(n, 1) * sizeof(T));
+}
+
+}  // namespace
+
+Denoiser::~Denoiser() { release(); }
+
+void Denoiser::release() {
+    for (void *p : owned_) cudaFree(p);
+    owned_.clear();
+    act_.clear();
+    grad_.clear();
+    cap_pixels_ = 0;
+}
+
+template <class T>
+cudaError_t Denoiser::take(T *&p, size_t n) {
+    cudaError_t e = dalloc(p, n);
+    if (e == cudaSuccess) owned_.push_back(p);
+    return e;
+}
+
+cudaError_t Denoiser::init(uint64_t seed) {
+    convs_.resize(kNumConvs);
+    size_t total = 0;
+    for (int i = 0; i < kNumConvs; i++) {
+        Conv &c = convs_[i];
+        c.cin = kConvs[i][0];
+        c.cout = kConvs[i][1];
+        c.relu = kConvs[i][2] != 0;
+        c.offset = total;
+        total += (size_t)c.cout * 9 * c.cin + c.cout;
+    }
+    n_params_ = total;
+    cudaError_t e;
+    if ((e = take(w_, total)) != cudaSuccess || (e = take(g_, total)) != cudaSuccess ||
+        (e = take(m_, total)) != cudaSuccess || (e = take(v_, total)) != cudaSuccess ||
+        (e = take(wb_, total)) != cudaSuccess || (e = take(loss_, 1)) != cudaSuccess)
+        return e;
+    // He-normal weights, zero biases, from the seed
+    std::vector<float> h(total, 0.f);
+    std::mt19937_64 rng(seed);
+    for (const Conv &c : convs_) {
+        std::normal_distribution<float> nd(0.f, std::sqrt(2.f / (9.f * c.cin)));
+        const size_t nw = (size_t)c.cout * 9 * c.cin;
+        for (size_t k = 0; k < nw; k++) h[c.offset + k] = nd(rng);
+    }
+    std::vector<float> zeros(total, 0.f);
+    if ((e = cudaMemcpy(w_, h.data(), total * 4, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(m_, zeros.data(), total * 4, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(v_, zeros.data(), total * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
+        return e;
+    step_ = 0;
+    return dn::to_bf16(w_, wb_, total, 0);
+}
+
+cudaError_t Denoiser::set_params(const float *host) {
+    cudaError_t e = cudaMemcpy(w_, host, n_params_ * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    return dn::to_bf16(w_, wb_, n_params_, 0);
+}
+
+cudaError_t Denoiser::get_params(float *host) const {
+    return cudaMemcpy(host, w_, n_params_ * 4, cudaMemcpyDeviceToHost);
+}
+
+cudaError_t Denoiser::get_grads(float *host) const {
+    return cudaMemcpy(host, g_, n_params_ * 4, cudaMemcpyDeviceToHost);
+}
+
+// Activation and gradient buffers for n images of h x w (h, w multiples of 16).
+cudaError_t Denoiser::ensure(int n, int h, int w) {
+    const size_t px = (size_t)n * h * w;
+    if (px <= cap_pixels_ && h == h_ && w == w_dim_ && n == n_) return cudaSuccess;
+    // keep the parameters, drop the activations
+    std::vector<void *> keep = {w_, g_, m_, v_, wb_, loss_};
+    for (void *p : owned_)
+        if (std::find(keep.begin(), keep.end(), p) == keep.end()) cudaFree(p);
+    owned_ = keep;
+    act_.clear();
+    grad_.clear();
+    n_ = n, h_ = h, w_dim_ = w;
+    cudaError_t e;
+    auto act = [&](int level, int c, bool with_grad) -> cudaError_t {
+        const size_t p = (size_t)n * (h >> level) * (w >> level);
+        Buf b;
+        b.level = level;
+        b.c = c;
+        cudaError_t er = take(b.x, p * c);
+        if (er != cudaSuccess) return er;
+        if (with_grad && (er = take(b.g, p * c)) != cudaSuccess) return er;
+        act_.push_back(b);
+        return cudaSuccess;
+    };
+    // act_ layout (index: tensor):
+    //  0 x0(10)
+    //  1 e0a 2 e0 | 3 p1 4 e1a 5 e1 | 6 p2 7 e2a 8 e2 | 9 p3 10 e3a 11 e3 | 12 p4 13 e4a 14 e4
+    //  15 cat3 16 d3a 17 d3 | 18 cat2 19 d2a 20 d2 | 21 cat1 22 d1a 23 d1 | 24 cat0 25 d0a 26 d0
+    if ((e = act(0, 10, false)) != cudaSuccess) return e;
+    for (int l = 0; l < 5; l++) {
+        if (l > 0 && (e = act(l, kEnc[l - 1], true)) != cudaSuccess) return e;  // pooled input
+        if ((e = act(l, kEnc[l], true)) != cudaSuccess) return e;
+        if ((e = act(l, kEnc[l], true)) != cudaSuccess) return e;
+    }
+    for (int l = 3; l >= 0; l--) {
+        const int up = (l == 3) ? kEnc[4] : kEnc[l + 1];
+        if ((e = act(l, up + kEnc[l], true)) != cudaSuccess) return e;  // concat
+        if ((e = act(l, kEnc[l], true)) != cudaSuccess) return e;
+        if ((e = act(l, kEnc[l], true)) != cudaSuccess) return e;
+    }
+    if ((e = take(out_, px * 3)) != cudaSuccess || (e = take(gout_, px * 3)) != cudaSuccess ||
+        (e = take(gtmp_, px * 128)) != cudaSuccess)
+        return e;
+    cap_pixels_ = px;
+    return cudaSuccess;
+}
+
+cudaError_t Denoiser::conv_fwd(int ci, const Buf &in, Buf &out, cudaStream_t st) {
+    const Conv &c = convs_[ci];
+    return dn::conv3x3_forward(in.x, wb_ + c.offset, w_ + c.offset + (size_t)c.cout * 9 * c.cin, out.x, nullptr, n_,
+                               h_ >> in.level, w_dim_ >> in.level, c.cin, c.cout, c.relu, st);
+}
+
+cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h, int w, cudaStream_t st) {
+    if (h % 16 || w % 16 || n <= 0) return cudaErrorInvalidValue;
+    cudaError_t e = ensure(n, h, w);
+    if (e != cudaSuccess) return e;
+    const size_t px = (size_t)n * h * w;
+    auto chk = [&](cudaError_t x) { if (x != cudaSuccess && e == cudaSuccess) e = x; };
+    chk(dn::pack_input(rad, feat, act_[0].x, px, st));
+    int conv = 0;
+    // encoder
+    int idx = 1, prev = 0;
+    for (int l = 0; l < 5; l++) {
+        if (l > 0) {
+            const Buf &src = act_[prev];
+            chk(dn::avgpool(src.x, act_[idx].x, n, h >> (l - 1), w >> (l - 1), src.c, st));
+            prev = idx++;
+        }
+        chk(conv_fwd(conv++, act_[prev], act_[idx], st));
+        prev = idx++;
+        chk(conv_fwd(conv++, act_[prev], act_[idx], st));
+        prev = idx++;
+    }
+    // decoder: prev = e4 (index 14)
+    const int skip_idx[4] = {11, 8, 5, 2};  // e3, e2, e1, e0
+    for (int k = 0; k < 4; k++) {
+        const int l = 3 - k;
+        Buf &cat = act_[idx];
+        const Buf &low = act_[prev];
+        const Buf &skip = act_[skip_idx[k]];
+        const size_t p = (size_t)n * (h >> l) * (w >> l);
+        chk(dn::upsample(low.x, cat.x, n, h >> (l + 1), w >> (l + 1), low.c, cat.c, st));
+        chk(dn::concat(skip.x, cat.x, p, skip.c, cat.c, low.c, st));
+        prev = idx++;
+        chk(conv_fwd(conv++, act_[prev], act_[idx], st));
+        prev = idx++;
+        chk(conv_fwd(conv++, act_[prev], act_[idx], st));
+        prev = idx++;
+    }
+    // output convolution (no ReLU), FP32
+    const Conv &c = convs_[conv];
+    chk(dn::conv3x3_forward(act_[prev].x, wb_ + c.offset, w_ + c.offset + (size_t)c.cout * 9 * c.cin, nullptr, out_,
+                            n, h, w, c.cin, c.cout, false, st));
+    return e;
+}
+
+cudaError_t Denoiser::backward(const float *target, cudaStream_t st) {
+    const int n = n_, h = h_, w = w_dim_;
+    const size_t px = (size_t)n * h * w;
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) { if (x != cudaSuccess && e == cudaSuccess) e = x; };
+    chk(cudaMemsetAsync(g_, 0, n_params_ * 4, st));
+    chk(cudaMemsetAsync(loss_, 0, 4, st));
+    for (Buf &b : act_)
+        if (b.g) chk(cudaMemsetAsync(b.g, 0, (size_t)n * (h >> b.level) * (w >> b.level) * b.c * 4, st));
+    chk(dn::l1_loss(out_, target, gout_, loss_, px * 3, st));
+    auto conv_bwd = [&](int ci, Buf &in, const float *gpre, int level) {
+        const Conv &c = convs_[ci];
+        chk(dn::conv3x3_backward(in.x, wb_ + c.offset, gpre, in.g, g_ + c.offset,
+                                 g_ + c.offset + (size_t)c.cout * 9 * c.cin, n, h >> level, w >> level, c.cin, c.cout,
+                                 st));
+    };
+    // output conv: input d0 (26)
+    conv_bwd(18, act_[26], gout_, 0);
+    // layer tensor i was produced by conv j from tensor i-1 (within a level)
+    // backward through (conv j: i-1 -> i) with the ReLU mask on i's gradient
+    auto through = [&](int ci, int out_idx) {
+        Buf &o = act_[out_idx];
+        const size_t p = (size_t)n * (h >> o.level) * (w >> o.level);
+        chk(dn::relu_mask(o.x, o.g, gtmp_, p * o.c, st));
+        conv_bwd(ci, act_[out_idx - 1], gtmp_, o.level);
+    };
+    const int skip_idx[4] = {11, 8, 5, 2};
+    // decoder, deepest last in forward => first here: d0 (convs 16,17), d1 (14,15), d2 (12,13), d3 (10,11)
+    for (int k = 3; k >= 0; k--) {
+        const int l = 3 - k;
+        const int cat_idx = 15 + 3 * k;
+        through(11 + 2 * k - 0 + 0 * l, cat_idx + 2);  // second conv of the level
+        through(10 + 2 * k, cat_idx + 1);              // first conv (input: concat)
+        Buf &cat = act_[cat_idx];
+        const Buf &skip = act_[skip_idx[k]];
+        const int low_idx = (k == 0) ? 14 : cat_idx - 1;  // e4 or the previous level's second conv
+        Buf &low = act_[low_idx];
+        const size_t p = (size_t)n * (h >> l) * (w >> l);
+        chk(dn::split_add(cat.g, act_[skip_idx[k]].g, p, skip.c, cat.c, low.c, st));
+        chk(dn::upsample_backward(cat.g, low.g, n, h >> (l + 1), w >> (l + 1), low.c, cat.c, st));
+    }
+    // encoder, deepest first: level l tensors: pooled (l>0), a, b
+    for (int l = 4; l >= 0; l--) {
+        const int b_idx = (l == 0) ? 2 : 3 * l + 2;
+        through(2 * l + 1, b_idx);
+        if (l == 0) {
+            // first conv's input is x0 (no gradient needed): weights only
+            Buf &o = act_[1];
+            const size_t p = (size_t)n * h * w;
+            chk(dn::relu_mask(o.x, o.g, gtmp_, p * o.c, st));
+            const Conv &c = convs_[0];
+            chk(dn::conv3x3_backward(act_[0].x, wb_ + c.offset, gtmp_, nullptr, g_ + c.offset,
+                                     g_ + c.offset + (size_t)c.cout * 9 * c.cin, n, h, w, c.cin, c.cout, st));
+        } else {
+            through(2 * l, b_idx - 1);
+            // pooled tensor (b_idx - 2) came from the previous level's output
+            const int src = (l == 1) ? 2 : 3 * (l - 1) + 2;
+            const Buf &pooled = act_[b_idx - 2];
+            chk(dn::avgpool_backward(pooled.g, act_[src].g, n, h >> (l - 1), w >> (l - 1), pooled.c, st));
+        }
+    }
+    return e;
+}
+
+cudaError_t Denoiser::apply_adam(float lr, cudaStream_t st) {
+    step_++;
+    return dn::adam(w_, g_, m_, v_, wb_, n_params_, lr, 0.9f, 0.999f, 1e-8f, step_, st);
+}
+
+cudaError_t Denoiser::output_radiance(float *out, cudaStream_t st) {
+    return dn::expm1_out(out_, out, (size_t)n_ * h_ * w_dim_ * 3, st);
+}
+
+}  // namespace pray_gpu

@@ -1,0 +1,62 @@
+// U-Net denoiser state on one device (denoise_net.cpp).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "denoise_ops.h"
+
+namespace pray_gpu {
+
+class Denoiser {
+  public:
+    ~Denoiser();
+    cudaError_t init(uint64_t seed);
+    size_t num_params() const { return n_params_; }
+    cudaError_t set_params(const float *host);
+    cudaError_t get_params(float *host) const;
+    cudaError_t get_grads(float *host) const;
+    // radiance: n*h*w*3 floats, feat: n*h*w*7 halves (albedo, normal, depth);
+    // h and w multiples of 16. The network output stays on the device.
+    cudaError_t forward(const float *rad, const __half *feat, int n, int h, int w, cudaStream_t st);
+    // after forward: L1 loss against the target radiance, all gradients
+    cudaError_t backward(const float *target, cudaStream_t st);
+    cudaError_t apply_adam(float lr, cudaStream_t st);
+    cudaError_t output_radiance(float *out, cudaStream_t st);
+    const float *loss_device() const { return loss_; }
+    int device = 0;
+
+  private:
+    struct Conv {
+        int cin, cout;
+        bool relu;
+        size_t offset;  // weights [cout][9][cin] then bias [cout] in the parameter vector
+    };
+    struct Buf {
+        int level = 0, c = 0;
+        __nv_bfloat16 *x = nullptr;
+        float *g = nullptr;
+    };
+    template <class T>
+    cudaError_t take(T *&p, size_t n);
+    cudaError_t ensure(int n, int h, int w);
+    cudaError_t conv_fwd(int ci, const Buf &in, Buf &out, cudaStream_t st);
+    void release();
+
+    std::vector<Conv> convs_;
+    std::vector<Buf> act_;
+    std::vector<float *> grad_;
+    std::vector<void *> owned_;
+    size_t n_params_ = 0, cap_pixels_ = 0;
+    int n_ = 0, h_ = 0, w_dim_ = 0, step_ = 0;
+    float *w_ = nullptr, *g_ = nullptr, *m_ = nullptr, *v_ = nullptr, *loss_ = nullptr;
+    __nv_bfloat16 *wb_ = nullptr;
+    float *out_ = nullptr, *gout_ = nullptr, *gtmp_ = nullptr;
+};
+
+}  // namespace pray_gpu

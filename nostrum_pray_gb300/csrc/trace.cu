@@ -4,6 +4,7 @@
 #include <cfloat>
 #include <cstdint>
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "device_layout.h"
@@ -131,7 +132,34 @@ __global__ void __launch_bounds__(128) k_render_rt(DevScene s, RtLaunch L) {
     }
 }
 
+// First-hit features of each pixel for the denoiser: albedo (or emitted
+// colour) 3, geometric normal 3, hit distance 1, as FP16; zeros on a miss.
+__global__ void __launch_bounds__(128) k_features(DevScene s, CameraConsts cam, float eps, __half *out) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t px, py;
+    const bool active = pixel_of(i, cam.width, cam.height, px, py);
+    const RayF r = primary_ray(cam, active ? px : 0, active ? py : 0);
+    float t = FLT_MAX;
+    const int pos = traverse<false>(s, r, eps, 0.f, active && s.n_refs > 0, t);
+    if (!active) return;
+    float f[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (pos >= 0) {
+        const int id = (int)__float_as_uint(__ldg(&s.tris[pos].v0[3]));
+        const float4 nrm = __ldg(reinterpret_cast<const float4 *>(s.shade[id].n));
+        const float4 col = __ldg(reinterpret_cast<const float4 *>(s.shade[id].c));
+        f[0] = col.x, f[1] = col.y, f[2] = col.z, f[3] = nrm.x, f[4] = nrm.y, f[5] = nrm.z, f[6] = t;
+    }
+    __half *o = out + 7ull * ((uint64_t)py * cam.width + px);
+    for (int k = 0; k < 7; k++) o[k] = __float2half(f[k]);
+}
+
 }  // namespace
+
+cudaError_t launch_features(const DevScene &s, const CameraConsts &cam, float eps, __half *out, cudaStream_t stream) {
+    const uint64_t threads = (uint64_t)((cam.width + 7) / 8) * ((cam.height + 3) / 4) * 32;
+    k_features<<<(unsigned)((threads + 127) / 128), 128, 0, stream>>>(s, cam, eps, out);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_trace_closest(const DevScene &s, const float *rays, uint64_t n, float eps, int32_t *ids,
                                  float *ts, cudaStream_t stream) {

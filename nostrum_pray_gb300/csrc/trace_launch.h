@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <string>
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "device_layout.h"
@@ -77,6 +78,8 @@ uint64_t noalloc_max_pixels();
 
 cudaError_t launch_relmse(const double *img, double img_scale, const double *ref, double ref_scale, uint64_t n,
                           double *out, cudaStream_t stream);
+
+cudaError_t launch_features(const DevScene &s, const CameraConsts &cam, float eps, __half *out, cudaStream_t stream);
 
 cudaError_t launch_trace_closest(const DevScene &s, const float *rays, uint64_t n, float eps, int32_t *ids,
                                  float *ts, cudaStream_t stream);

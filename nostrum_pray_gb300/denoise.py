@@ -1,0 +1,190 @@
+"""Learned denoising on top of the path tracer: data generation, training and
+evaluation of the U-Net (pray_denoiser_* in include/nostrum_pray.h).
+
+Data: seeded procedural rooms (scenes.random_room), each rendered with the
+next-event-estimation path tracer at a few samples per pixel (the noisy
+input), with its first-hit features, and at many samples per pixel
+accumulated in FP64 (the reference). The network is trained by its own CUDA
+forward/backward kernels with an L1 loss in log(1 + radiance) space and Adam.
+
+Evaluation on held-out rooms: relMSE (mean over pixels and channels of
+(x - r)^2 / (r^2 + 0.01), FP64 on the GPU) of the noisy input, the denoised
+image and plain renders at increasing sample counts; the time each needs to
+reach relMSE <= 0.01; and a fallback: when the predicted error of a denoised
+image (half the relMSE between the denoised results of two independent
+renders) exceeds the target, the image is re-rendered plainly at the sample
+count that reached the target on the training rooms.
+"""
+from __future__ import annotations
+
+import dataclasses
+import time
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+
+from . import native, scenes
+
+
+@dataclasses.dataclass
+class DenoiseConfig:
+    res: int = 128
+    spp_in: int = 4
+    spp_ref: int = 1024
+    depth: int = 8
+    rr_depth: int = 3
+    train_rooms: int = 96
+    eval_rooms: int = 16
+    room_grid: int = 16
+    steps: int = 1000
+    batch: int = 8
+    lr: float = 1e-3
+    target: float = 0.01
+    seed: int = 1000
+
+
+def _setup(cfg: DenoiseConfig):
+    return scenes.room_setup(cfg.res, cfg.res, spp=cfg.spp_in, max_depth=cfg.depth)
+
+
+def _params(cfg, st, spp, seed, offset=0):
+    return native.pt_params(st, spp=spp, max_depth=cfg.depth, seed=seed, mode=native.PT_NEE,
+                            rr_depth=cfg.rr_depth, scheduler=native.SCHED_WAVEFRONT, sample_offset=offset)
+
+
+def render_room(cfg: DenoiseConfig, room_seed: int, torch):
+    """(scene, noisy radiance, features, reference radiance FP64) on the device."""
+    st = _setup(cfg)
+    sc = native.Scene.from_setup(scenes.random_room(room_seed, grid=cfg.room_grid), st)
+    h = w = cfg.res
+    rad = torch.empty((h, w, 3), dtype=torch.float32, device="cuda")
+    rgb = torch.empty((h, w, 3), dtype=torch.uint8, device="cuda")
+    sc.render_pt(_params(cfg, st, cfg.spp_in, seed=room_seed * 7 + 1), rgb, rad)
+    feat = torch.empty((h, w, 7), dtype=torch.float16, device="cuda")
+    sc.render_features(_params(cfg, st, 1, seed=0), feat)
+    ref = torch.zeros((h, w, 3), dtype=torch.float64, device="cuda")
+    chunk = 256
+    for off in range(0, cfg.spp_ref, chunk):
+        sc.accumulate_pt(_params(cfg, st, min(chunk, cfg.spp_ref - off), seed=room_seed * 7 + 2, offset=off), ref)
+    ref /= cfg.spp_ref
+    return sc, rad, feat, ref
+
+
+def relmse(img, ref, torch) -> float:
+    """FP64 relMSE on the device (pray_relmse)."""
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    native.relmse(img.to(torch.float64).contiguous(), 1.0, ref.contiguous(), 1.0, out)
+    return float(out.item())
+
+
+def make_dataset(cfg: DenoiseConfig, seeds: List[int], torch):
+    rads, feats, refs, scs = [], [], [], []
+    for s in seeds:
+        sc, rad, feat, ref = render_room(cfg, s, torch)
+        rads.append(rad)
+        feats.append(feat)
+        refs.append(ref)
+        scs.append(sc)
+    return scs, torch.stack(rads), torch.stack(feats), torch.stack(refs)
+
+
+def train(den: native.Denoiser, rad, feat, ref, cfg: DenoiseConfig, torch, log_every: int = 100):
+    n = rad.shape[0]
+    target = ref.to(torch.float32)
+    g = torch.Generator(device="cpu").manual_seed(cfg.seed)
+    losses = []
+    for step in range(cfg.steps):
+        idx = torch.randperm(n, generator=g)[:cfg.batch].cuda()
+        r, f, t = rad.index_select(0, idx), feat.index_select(0, idx), target.index_select(0, idx)
+        # random flips keep the data small but varied
+        if step % 2:
+            r, f, t = r.flip(2), f.flip(2), t.flip(2)
+        want = (step % log_every == 0) or step == cfg.steps - 1
+        loss = den.train_step(r.contiguous(), f.contiguous(), t.contiguous(), cfg.lr, want_loss=want)
+        if want:
+            losses.append((step, loss))
+    return losses
+
+
+def timed(fn, torch) -> float:
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / 1e3
+
+
+def plain_curve(cfg: DenoiseConfig, sc, ref, room_seed: int, torch, spps=(4, 8, 16, 32, 64, 128, 256, 512)):
+    """relMSE and render time of plain renders at each sample count (seeds
+    independent of the reference's)."""
+    st = _setup(cfg)
+    out = []
+    rad = torch.empty((cfg.res, cfg.res, 3), dtype=torch.float32, device="cuda")
+    for spp in spps:
+        p = _params(cfg, st, spp, seed=room_seed * 7 + 3)
+        sc.render_pt(p, None, rad)  # warm (graph capture)
+        t = timed(lambda: sc.render_pt(p, None, rad), torch)
+        out.append((spp, relmse(rad, ref, torch), t))
+    return out
+
+
+def denoised_eval(cfg: DenoiseConfig, den, sc, ref, room_seed: int, torch):
+    """Denoised relMSE, time (render + features + inference) and predicted
+    error from two independent renders."""
+    st = _setup(cfg)
+    h = w = cfg.res
+    rad = torch.empty((1, h, w, 3), dtype=torch.float32, device="cuda")
+    rad2 = torch.empty((1, h, w, 3), dtype=torch.float32, device="cuda")
+    feat = torch.empty((1, h, w, 7), dtype=torch.float16, device="cuda")
+    out = torch.empty((1, h, w, 3), dtype=torch.float32, device="cuda")
+    out2 = torch.empty((1, h, w, 3), dtype=torch.float32, device="cuda")
+    p = _params(cfg, st, cfg.spp_in, seed=room_seed * 7 + 5)
+    p2 = _params(cfg, st, cfg.spp_in, seed=room_seed * 7 + 6)
+    pf = _params(cfg, st, 1, seed=0)
+
+    def run():
+        sc.render_pt(p, None, rad[0])
+        sc.render_features(pf, feat[0])
+        den.denoise(rad, feat, out)
+
+    run()
+    t = timed(run, torch)
+    e = relmse(out[0], ref, torch)
+    e_noisy = relmse(rad[0], ref, torch)
+    sc.render_pt(p2, None, rad2[0])
+    den.denoise(rad2, feat, out2)
+    pred = 0.5 * relmse(out[0], out2[0].to(torch.float64), torch)
+    return {"relmse_denoised": e, "relmse_noisy": e_noisy, "time_s": t, "predicted": pred}
+
+
+def evaluate(cfg: DenoiseConfig, den, eval_rooms, torch, fallback_spp: int) -> Dict:
+    rows = []
+    for seed, (sc, ref) in eval_rooms.items():
+        curve = plain_curve(cfg, sc, ref, seed, torch)
+        plain_ok = [(spp, e, t) for spp, e, t in curve if e <= cfg.target]
+        d = denoised_eval(cfg, den, sc, ref, seed, torch)
+        t_plain = plain_ok[0][2] if plain_ok else float("nan")
+        spp_plain = plain_ok[0][0] if plain_ok else None
+        # fallback: predicted error above target -> plain render at the calibrated spp
+        t_final, e_final, used_fallback = d["time_s"], d["relmse_denoised"], False
+        if d["predicted"] > cfg.target:
+            used_fallback = True
+            fb = [(spp, e, t) for spp, e, t in curve if spp == fallback_spp]
+            if fb:
+                t_final = d["time_s"] + fb[0][2]
+                e_final = fb[0][1]
+        rows.append({"seed": seed, "spp_plain_to_target": spp_plain, "time_plain_s": t_plain, **d,
+                     "fallback": used_fallback, "time_final_s": t_final, "relmse_final": e_final})
+    return {"rooms": rows}
+
+
+def fallback_spp_from(curves: List[List[Tuple[int, float, float]]], target: float) -> int:
+    """Smallest sample count whose plain relMSE reached the target on every
+    calibration room (the largest tried if none did)."""
+    spps = [c[0] for c in curves[0]]
+    for i, spp in enumerate(spps):
+        if all(c[i][1] <= target for c in curves):
+            return spp
+    return spps[-1]

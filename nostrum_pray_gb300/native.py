@@ -75,6 +75,9 @@ EXPORTED = [
     "pray_render_rt", "pray_render_rt_host", "pray_render_rt_counts", "pray_render_pt", "pray_render_pt_host",
     "pray_accumulate_pt", "pray_relmse", "pray_render_pt_noalloc",
     "pray_batch_create", "pray_batch_destroy", "pray_batch_set_config", "pray_batch_tune", "pray_batch_render",
+    "pray_render_features", "pray_denoiser_create", "pray_denoiser_destroy", "pray_denoiser_num_params",
+    "pray_denoiser_get_params", "pray_denoiser_set_params", "pray_denoise", "pray_denoiser_train_step",
+    "pray_denoiser_gradients",
 ]
 
 
@@ -111,6 +114,15 @@ def lib():
         L.pray_batch_set_config.argtypes = [_vp, ctypes.POINTER(BatchConfig)]
         L.pray_batch_tune.argtypes = [_vp, ctypes.POINTER(BatchConfig), ctypes.POINTER(_f32)]
         L.pray_batch_render.argtypes = [_vp, _vp, _vp]
+        L.pray_render_features.argtypes = [_vp, ctypes.POINTER(PtParams), _vp, _vp]
+        L.pray_denoiser_create.argtypes = [_i32, _u64, ctypes.POINTER(_vp)]
+        L.pray_denoiser_destroy.argtypes = [_vp]
+        L.pray_denoiser_num_params.argtypes = [_vp, ctypes.POINTER(_u64)]
+        L.pray_denoiser_get_params.argtypes = [_vp, _vp]
+        L.pray_denoiser_set_params.argtypes = [_vp, _vp]
+        L.pray_denoise.argtypes = [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp]
+        L.pray_denoiser_train_step.argtypes = [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _f32, _vp, _vp]
+        L.pray_denoiser_gradients.argtypes = [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp]
         L.pray_relmse.argtypes = [_vp, ctypes.c_double, _vp, ctypes.c_double, _u64, _vp, _vp]
         for name in EXPORTED:
             if not hasattr(L, name):
@@ -274,6 +286,10 @@ class Scene:
         check(lib().pray_render_pt_noalloc(self._h, ctypes.byref(params), _ptr(rgb), _ptr(radiance), _ptr(counters),
                                            _stream(stream)))
 
+    def render_features(self, params: PtParams, features, stream=None) -> None:
+        """First-hit albedo, normal, distance as FP16 (torch.float16 h x w x 7)."""
+        check(lib().pray_render_features(self._h, ctypes.byref(params), _ptr(features), _stream(stream)))
+
     def accumulate_pt(self, params: PtParams, sum64, counters=None, stream=None) -> None:
         check(lib().pray_accumulate_pt(self._h, ctypes.byref(params), _ptr(sum64), _ptr(counters), _stream(stream)))
 
@@ -357,3 +373,53 @@ class Batch:
 
     def render(self, counters=None, stream=None) -> None:
         check(lib().pray_batch_render(self._h, _ptr(counters), _stream(stream)))
+
+
+class Denoiser:
+    """The U-Net denoiser (pray_denoiser_*). Tensors are torch CUDA tensors:
+    radiance (n, h, w, 3) float32, features (n, h, w, 7) float16."""
+
+    def __init__(self, seed: int = 0, device: int = 0):
+        h = _vp()
+        check(lib().pray_denoiser_create(device, seed, ctypes.byref(h)))
+        self._h = h
+        n = _u64()
+        check(lib().pray_denoiser_num_params(self._h, ctypes.byref(n)))
+        self.num_params = n.value
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.pray_denoiser_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.num_params, np.float32)
+        check(lib().pray_denoiser_get_params(self._h, out.ctypes.data))
+        return out
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.num_params
+        check(lib().pray_denoiser_set_params(self._h, p.ctypes.data))
+
+    def denoise(self, radiance, features, out, stream=None) -> None:
+        n, h, w, _ = radiance.shape
+        check(lib().pray_denoise(self._h, _ptr(radiance), _ptr(features), n, h, w, _ptr(out), _stream(stream)))
+
+    def train_step(self, radiance, features, target, lr: float, want_loss: bool = False, stream=None):
+        n, h, w, _ = radiance.shape
+        loss = np.zeros(1, np.float32)
+        check(lib().pray_denoiser_train_step(self._h, _ptr(radiance), _ptr(features), _ptr(target), n, h, w, lr,
+                                             loss.ctypes.data if want_loss else None, _stream(stream)))
+        return float(loss[0]) if want_loss else None
+
+    def gradients(self, radiance, features, target):
+        n, h, w, _ = radiance.shape
+        loss = np.zeros(1, np.float32)
+        g = np.empty(self.num_params, np.float32)
+        check(lib().pray_denoiser_gradients(self._h, _ptr(radiance), _ptr(features), _ptr(target), n, h, w,
+                                            loss.ctypes.data, g.ctypes.data))
+        return float(loss[0]), g

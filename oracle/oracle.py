@@ -36,11 +36,12 @@ _u64 = ctypes.c_uint64
 
 def build(verbose: bool = False) -> str:
     """Compiles pray_oracle.cpp (no FMA contraction, OpenMP) if stale."""
-    src = os.path.join(HERE, "pray_oracle.cpp")
+    srcs = [os.path.join(HERE, "pray_oracle.cpp"), os.path.join(HERE, "denoise_oracle.cpp")]
+    deps = srcs + [os.path.join(os.path.dirname(HERE), "include", "nostrum_pray_sampling.h")]
     os.makedirs(BUILD_DIR, exist_ok=True)
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(d) for d in deps):
         cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
-               src, "-o", LIB + ".tmp"]
+               *srcs, "-o", LIB + ".tmp"]
         subprocess.run(cmd, check=True, capture_output=not verbose)
         os.replace(LIB + ".tmp", LIB)
     return LIB
@@ -70,6 +71,10 @@ def lib():
         L.orc_render_rt.argtypes = [_vp, _u64, _u64, _u64, _f32p, _f32p, _f32p, ctypes.c_int, _f32p,
                                     ctypes.c_float, _u64, _u64, _u8p, ctypes.c_int]
         L.orc_sincos_turns.argtypes = [_f32p, _u64, _f32p, _f32p]
+        L.orc_unet_num_params.restype = _u64
+        L.orc_unet.restype = ctypes.c_double
+        L.orc_unet.argtypes = [_f32p, _f32p, np.ctypeslib.ndpointer(np.uint16, flags="C_CONTIGUOUS"), _f32p,
+                               ctypes.c_int, ctypes.c_int, ctypes.c_int, _f64p, _f64p]
         L.orc_sample_hemisphere.argtypes = [_f32p, _f32p, _u64, _f32p]
         L.orc_render_pt.restype = _u64
         L.orc_render_pt.argtypes = [_vp, _u64, _u64, _u64, _f32p, _f32p, _f32p, ctypes.c_uint32, ctypes.c_uint32,
@@ -97,6 +102,17 @@ def camera(width, height, fov, cam_pos, cam_look) -> np.ndarray:
     out = np.empty(13, np.float32)
     lib().orc_camera(width, height, fov, _f3(cam_pos), _f3(cam_look), out)
     return out
+
+
+def unet(params, rad, feat_f16, target):
+    """FP64 U-Net forward + L1 loss + backward: (loss, output, grads)."""
+    n, h, w, _ = rad.shape
+    out = np.empty((n, h, w, 3), np.float64)
+    g = np.empty(int(lib().orc_unet_num_params()), np.float64)
+    loss = lib().orc_unet(np.ascontiguousarray(params, np.float32), np.ascontiguousarray(rad, np.float32),
+                          np.ascontiguousarray(feat_f16).view(np.uint16), np.ascontiguousarray(target, np.float32),
+                          n, h, w, out, g)
+    return loss, out, g
 
 
 def sincos_turns(u: np.ndarray):

@@ -1,0 +1,88 @@
+"""Denoiser kernels against the FP64 oracle (oracle/denoise_oracle.cpp):
+network output, L1 loss and every parameter gradient, on random inputs;
+training on a fixed batch must reduce the loss; first-hit features must equal
+the oracle's hit data exactly."""
+import numpy as np
+import pytest
+
+from nostrum_pray_gb300 import native, scenes
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    native.lib()
+
+
+CONVS = [(10, 32), (32, 32), (32, 48), (48, 48), (48, 64), (64, 64), (64, 96), (96, 96), (96, 128), (128, 128),
+         (224, 96), (96, 96), (160, 64), (64, 64), (112, 48), (48, 48), (80, 32), (32, 32), (32, 3)]
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def random_batch(seed, n, h, w):
+    rng = np.random.default_rng(seed)
+    rad = (rng.random((n, h, w, 3)) * 2).astype(np.float32)
+    feat = rng.random((n, h, w, 7)).astype(np.float16)
+    tgt = rng.random((n, h, w, 3)).astype(np.float32)
+    return rad, feat, tgt
+
+
+def test_gradients_match_fp64_oracle(oracle):
+    den = native.Denoiser(seed=5)
+    params = den.get_params()
+    rad, feat, tgt = random_batch(1, 2, 32, 32)
+    t = lambda a: torch.from_numpy(a).cuda()
+    loss, g = den.gradients(t(rad), t(feat), t(tgt))
+    out = torch.empty((2, 32, 32, 3), dtype=torch.float32, device="cuda")
+    den.denoise(t(rad), t(feat), out)
+    torch.cuda.synchronize()
+    oloss, oout, og = oracle.unet(params, rad, feat, tgt)
+    assert abs(loss - oloss) <= 2e-3 * abs(oloss)
+    assert rel(np.log1p(out.cpu().numpy().astype(np.float64)), oout) < 5e-3
+    off = 0
+    for cin, cout in CONVS:
+        nw = cout * 9 * cin
+        assert rel(g[off:off + nw], og[off:off + nw]) < 3e-2, (cin, cout)
+        assert rel(g[off + nw:off + nw + cout], og[off + nw:off + nw + cout]) < 3e-2, (cin, cout, "bias")
+        off += nw + cout
+    assert off == den.num_params
+
+
+def test_training_reduces_loss():
+    den = native.Denoiser(seed=2)
+    rad, feat, tgt = random_batch(3, 4, 32, 32)
+    tgt = np.clip(rad * 0.5 + 0.1, 0, None).astype(np.float32)  # learnable map
+    t = lambda a: torch.from_numpy(a).cuda()
+    rad_t, feat_t, tgt_t = t(rad), t(feat), t(tgt)
+    first = den.train_step(rad_t, feat_t, tgt_t, 1e-3, want_loss=True)
+    for _ in range(60):
+        den.train_step(rad_t, feat_t, tgt_t, 1e-3)
+    last = den.train_step(rad_t, feat_t, tgt_t, 1e-3, want_loss=True)
+    assert last < 0.5 * first, (first, last)
+
+
+def test_features_match_oracle_hits(oracle):
+    m = scenes.room(grid=6)
+    st = scenes.room_setup(48, 32)
+    sc = native.Scene.from_setup(m, st)
+    feat = torch.empty((32, 48, 7), dtype=torch.float16, device="cuda")
+    sc.render_features(native.pt_params(st, spp=1, max_depth=1), feat)
+    torch.cuda.synchronize()
+    got = feat.cpu().numpy().reshape(-1, 7)
+    orc = oracle.OracleScene.from_setup(m, st)
+    rays = oracle.primary_rays(st.width, st.height, st.fov, st.cam_pos, st.cam_look)
+    ids, ts = orc.trace(rays, st.det_eps)
+    pre = orc.precompute()
+    want = np.zeros((ids.size, 7), np.float32)
+    hit = ids >= 0
+    want[hit, 0:3] = m.colors[ids[hit]]
+    want[hit, 3:6] = pre[ids[hit], 15:18]
+    want[hit, 6] = ts[hit]
+    np.testing.assert_array_equal(got, want.astype(np.float16))
