@@ -260,7 +260,9 @@ typedef struct pray_denoiser pray_denoiser;
  * convolutions with ReLU per level, 2x2 average pooling, nearest 2x
  * upsampling, concatenated skips, 3x3 output convolution), BF16 weights and
  * activations, FP32 accumulation. Input per pixel: log(1 + noisy radiance),
- * the 7 features; output: radiance. Weights He-initialised from seed.
+ * the 7 features; output: radiance, as log(1 + noisy radiance) plus the
+ * network's correction. Weights He-initialised from seed (the output
+ * convolution scaled by 0.1, so an untrained network returns its input).
  * Parameter vector: per convolution in forward order, weights
  * [cout][3][3][cin] then biases [cout]. */
 pray_status pray_denoiser_create(int32_t device, uint64_t seed, pray_denoiser **out);
@@ -278,6 +280,12 @@ pray_status pray_denoise(pray_denoiser *d, const float *radiance_dev, const uint
 pray_status pray_denoiser_train_step(pray_denoiser *d, const float *radiance_dev, const uint16_t *features_dev,
                                      const float *target_dev, int32_t n, int32_t h, int32_t w, float lr,
                                      float *loss_host, void *stream);
+/* Forward convolutions on the tcgen05 tensor cores (enable != 0, the
+ * default) or on the CUDA cores. The backward pass runs on the CUDA cores. */
+pray_status pray_denoiser_set_tensor_cores(pray_denoiser *d, int32_t enable);
+/* Synchronises and reports PRAY_ERR_CUDA if a tensor-core kernel's bounded
+ * wait on its MMA completion ran out since the denoiser was created. */
+pray_status pray_denoiser_check(pray_denoiser *d);
 /* Loss and parameter gradients without an update (synchronises):
  * grads_host has pray_denoiser_num_params floats. */
 pray_status pray_denoiser_gradients(pray_denoiser *d, const float *radiance_dev, const uint16_t *features_dev,

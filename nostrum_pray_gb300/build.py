@@ -21,7 +21,7 @@ CLI = os.path.join(BUILD, "Pray")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["trace.cu", "pt.cu", "wavefront.cu", "wavefront_noalloc.cu", "batch.cu", "denoise_ops.cu"]
+CU_SOURCES = ["trace.cu", "pt.cu", "wavefront.cu", "wavefront_noalloc.cu", "batch.cu", "denoise_ops.cu", "denoise_tc.cu"]
 CPP_SOURCES = ["capi.cpp", "host/kdtree.cpp", "host/camera.cpp", "host/flatten.cpp", "denoise_net.cpp"]
 CLI_SOURCES = ["cli/pray_main.cpp", "cli/scene_io.cpp"]
 DUMP_SOURCES = ["cli/scene_dump.cpp"]

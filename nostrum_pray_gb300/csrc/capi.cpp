@@ -1014,6 +1014,22 @@ pray_status pray_denoiser_train_step(pray_denoiser *d, const float *rad, const u
     return e == cudaSuccess ? PRAY_OK : cuda_error(e, "denoiser train step");
 }
 
+pray_status pray_denoiser_set_tensor_cores(pray_denoiser *d, int32_t enable) {
+    if (!d) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    d->net.set_tensor_cores(enable != 0);
+    return PRAY_OK;
+}
+
+pray_status pray_denoiser_check(pray_denoiser *d) {
+    if (!d) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    cudaSetDevice(d->net.device);
+    bool ok = true;
+    cudaError_t e = d->net.check(ok);
+    if (e != cudaSuccess) return cuda_error(e, "denoiser check");
+    if (!ok) return set_error(PRAY_ERR_CUDA, "a tensor-core convolution timed out waiting for its MMAs");
+    return PRAY_OK;
+}
+
 pray_status pray_denoiser_gradients(pray_denoiser *d, const float *rad, const uint16_t *feat, const float *target,
                                     int32_t n, int32_t h, int32_t w, float *loss_host, float *grads_host) {
     if (!d || !rad || !feat || !target || !grads_host) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");

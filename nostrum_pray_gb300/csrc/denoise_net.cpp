@@ -3,7 +3,8 @@
 // average pooling down, nearest 2x upsampling up, skip connections by channel
 // concatenation, a final 3x3 convolution to RGB). Input per pixel:
 // log(1 + radiance) of the noisy render (3), first-hit albedo (3), normal (3)
-// and depth (1); output: log(1 + radiance) of the estimate. Trained with an L1
+// and depth (1); output: log(1 + radiance) of the estimate, as the noisy
+// input's log(1 + radiance) plus the network's correction. Trained with an L1
 // loss in that log space and Adam. Every kernel is in denoise_ops.cu.
 #include "denoise_net.h"
 
@@ -71,13 +72,17 @@ cudaError_t Denoiser::init(uint64_t seed) {
     cudaError_t e;
     if ((e = take(w_, total)) != cudaSuccess || (e = take(g_, total)) != cudaSuccess ||
         (e = take(m_, total)) != cudaSuccess || (e = take(v_, total)) != cudaSuccess ||
-        (e = take(wb_, total)) != cudaSuccess || (e = take(loss_, 1)) != cudaSuccess)
+        (e = take(wb_, total)) != cudaSuccess || (e = take(loss_, 1)) != cudaSuccess ||
+        (e = take(err_, 1)) != cudaSuccess || (e = cudaMemset(err_, 0, sizeof(int))) != cudaSuccess)
         return e;
     // He-normal weights, zero biases, from the seed
     std::vector<float> h(total, 0.f);
     std::mt19937_64 rng(seed);
     for (const Conv &c : convs_) {
-        std::normal_distribution<float> nd(0.f, std::sqrt(2.f / (9.f * c.cin)));
+        // the output convolution starts small, so the initial estimate is the
+        // noisy input
+        const float scale = c.relu ? 1.f : 0.1f;
+        std::normal_distribution<float> nd(0.f, scale * std::sqrt(2.f / (9.f * c.cin)));
         const size_t nw = (size_t)c.cout * 9 * c.cin;
         for (size_t k = 0; k < nw; k++) h[c.offset + k] = nd(rng);
     }
@@ -109,7 +114,7 @@ cudaError_t Denoiser::ensure(int n, int h, int w) {
     const size_t px = (size_t)n * h * w;
     if (px <= cap_pixels_ && h == h_ && w == w_dim_ && n == n_) return cudaSuccess;
     // keep the parameters, drop the activations
-    std::vector<void *> keep = {w_, g_, m_, v_, wb_, loss_};
+    std::vector<void *> keep = {w_, g_, m_, v_, wb_, loss_, err_};
     for (void *p : owned_)
         if (std::find(keep.begin(), keep.end(), p) == keep.end()) cudaFree(p);
     owned_ = keep;
@@ -151,8 +156,19 @@ cudaError_t Denoiser::ensure(int n, int h, int w) {
     return cudaSuccess;
 }
 
+cudaError_t Denoiser::check(bool &ok) {
+    cudaError_t e = cudaDeviceSynchronize();
+    int flag = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&flag, err_, sizeof(int), cudaMemcpyDeviceToHost);
+    ok = flag == 0;
+    return e;
+}
+
 cudaError_t Denoiser::conv_fwd(int ci, const Buf &in, Buf &out, cudaStream_t st) {
     const Conv &c = convs_[ci];
+    if (tensor_cores_)
+        return dn::conv3x3_forward_tc(in.x, wb_ + c.offset, w_ + c.offset + (size_t)c.cout * 9 * c.cin, out.x, nullptr,
+                                      n_, h_ >> in.level, w_dim_ >> in.level, c.cin, c.cout, c.relu, err_, st);
     return dn::conv3x3_forward(in.x, wb_ + c.offset, w_ + c.offset + (size_t)c.cout * 9 * c.cin, out.x, nullptr, n_,
                                h_ >> in.level, w_dim_ >> in.level, c.cin, c.cout, c.relu, st);
 }
@@ -196,8 +212,14 @@ cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h
     }
     // output convolution (no ReLU), FP32
     const Conv &c = convs_[conv];
-    chk(dn::conv3x3_forward(act_[prev].x, wb_ + c.offset, w_ + c.offset + (size_t)c.cout * 9 * c.cin, nullptr, out_,
-                            n, h, w, c.cin, c.cout, false, st));
+    if (tensor_cores_)
+        chk(dn::conv3x3_forward_tc(act_[prev].x, wb_ + c.offset, w_ + c.offset + (size_t)c.cout * 9 * c.cin, nullptr,
+                                   out_, n, h, w, c.cin, c.cout, false, err_, st));
+    else
+        chk(dn::conv3x3_forward(act_[prev].x, wb_ + c.offset, w_ + c.offset + (size_t)c.cout * 9 * c.cin, nullptr,
+                                out_, n, h, w, c.cin, c.cout, false, st));
+    // the network predicts a correction to the noisy input's log radiance
+    chk(dn::add_input(out_, act_[0].x, px, st));
     return e;
 }
 

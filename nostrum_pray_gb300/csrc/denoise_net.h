@@ -29,6 +29,12 @@ class Denoiser {
     cudaError_t apply_adam(float lr, cudaStream_t st);
     cudaError_t output_radiance(float *out, cudaStream_t st);
     const float *loss_device() const { return loss_; }
+    // forward convolutions on the tcgen05 tensor cores (default) or on the
+    // CUDA cores
+    void set_tensor_cores(bool on) { tensor_cores_ = on; }
+    bool tensor_cores() const { return tensor_cores_; }
+    // synchronises; false if a tensor-core kernel reported a timed-out wait
+    cudaError_t check(bool &ok);
     int device = 0;
 
   private:
@@ -57,6 +63,8 @@ class Denoiser {
     float *w_ = nullptr, *g_ = nullptr, *m_ = nullptr, *v_ = nullptr, *loss_ = nullptr;
     __nv_bfloat16 *wb_ = nullptr;
     float *out_ = nullptr, *gout_ = nullptr, *gtmp_ = nullptr;
+    int *err_ = nullptr;
+    bool tensor_cores_ = true;
 };
 
 }  // namespace pray_gpu

@@ -290,6 +290,11 @@ __global__ void k_l1(const float *out, const float *target, float *g, float *los
     if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc * inv);
 }
 
+// residual output: out (log space) += the input's log(1 + radiance) channels
+__global__ void k_add_input(float *out, const __nv_bfloat16 *x0, size_t pixels) {
+    for (size_t i = gtid(); i < pixels * 3; i += gstride()) out[i] += bf(x0[(i / 3) * 10 + i % 3]);
+}
+
 __global__ void k_expm1(const float *out, float *rad, size_t n) {
     for (size_t i = gtid(); i < n; i += gstride()) rad[i] = expm1f(out[i]);
 }
@@ -376,6 +381,10 @@ cudaError_t pack_input(const float *rad, const __half *feat, __nv_bfloat16 *x, s
 }
 cudaError_t l1_loss(const float *out, const float *target, float *g, float *loss, size_t n, cudaStream_t st) {
     k_l1<<<blocks_for(n), 256, 0, st>>>(out, target, g, loss, n);
+    return cudaGetLastError();
+}
+cudaError_t add_input(float *out, const __nv_bfloat16 *x0, size_t pixels, cudaStream_t st) {
+    k_add_input<<<blocks_for(pixels * 3), 256, 0, st>>>(out, x0, pixels);
     return cudaGetLastError();
 }
 cudaError_t expm1_out(const float *out, float *rad, size_t n, cudaStream_t st) {

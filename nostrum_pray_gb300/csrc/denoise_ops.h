@@ -14,6 +14,11 @@
 namespace pray_gpu {
 namespace dn {
 
+// tcgen05 tensor-core version (denoise_tc.cu); *err is set to 1 if one of
+// its bounded mbarrier waits ran out
+cudaError_t conv3x3_forward_tc(const __nv_bfloat16 *x, const __nv_bfloat16 *w, const float *b, __nv_bfloat16 *y,
+                               float *y32, int n, int h, int wd, int cin, int cout, bool relu, int *err,
+                               cudaStream_t st);
 cudaError_t conv3x3_forward(const __nv_bfloat16 *x, const __nv_bfloat16 *w, const float *b, __nv_bfloat16 *y,
                             float *y32, int n, int h, int wd, int cin, int cout, bool relu, cudaStream_t st);
 // gpre: output gradient after the ReLU mask (FP32, n*h*w*cout); dx may be NULL
@@ -28,6 +33,7 @@ cudaError_t concat(const __nv_bfloat16 *x, __nv_bfloat16 *y, size_t pixels, int 
 cudaError_t split_add(const float *gy, float *gx, size_t pixels, int c, int cy, int off, cudaStream_t st);
 cudaError_t pack_input(const float *rad, const __half *feat, __nv_bfloat16 *x, size_t pixels, cudaStream_t st);
 cudaError_t l1_loss(const float *out, const float *target, float *g, float *loss, size_t n, cudaStream_t st);
+cudaError_t add_input(float *out, const __nv_bfloat16 *x0, size_t pixels, cudaStream_t st);
 cudaError_t expm1_out(const float *out, float *rad, size_t n, cudaStream_t st);
 cudaError_t adam(float *w, const float *g, float *m, float *v, __nv_bfloat16 *wb, size_t n, float lr, float b1,
                  float b2, float eps, int step, cudaStream_t st);

@@ -100,7 +100,8 @@ def train(den: native.Denoiser, rad, feat, ref, cfg: DenoiseConfig, torch, log_e
         if step % 2:
             r, f, t = r.flip(2), f.flip(2), t.flip(2)
         want = (step % log_every == 0) or step == cfg.steps - 1
-        loss = den.train_step(r.contiguous(), f.contiguous(), t.contiguous(), cfg.lr, want_loss=want)
+        lr = cfg.lr * 0.5 * (1.0 + np.cos(np.pi * step / cfg.steps))  # cosine decay
+        loss = den.train_step(r.contiguous(), f.contiguous(), t.contiguous(), lr, want_loss=want)
         if want:
             losses.append((step, loss))
     return losses

@@ -77,7 +77,7 @@ EXPORTED = [
     "pray_batch_create", "pray_batch_destroy", "pray_batch_set_config", "pray_batch_tune", "pray_batch_render",
     "pray_render_features", "pray_denoiser_create", "pray_denoiser_destroy", "pray_denoiser_num_params",
     "pray_denoiser_get_params", "pray_denoiser_set_params", "pray_denoise", "pray_denoiser_train_step",
-    "pray_denoiser_gradients",
+    "pray_denoiser_gradients", "pray_denoiser_set_tensor_cores", "pray_denoiser_check",
 ]
 
 
@@ -122,6 +122,8 @@ def lib():
         L.pray_denoiser_set_params.argtypes = [_vp, _vp]
         L.pray_denoise.argtypes = [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp]
         L.pray_denoiser_train_step.argtypes = [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _f32, _vp, _vp]
+        L.pray_denoiser_set_tensor_cores.argtypes = [_vp, _i32]
+        L.pray_denoiser_check.argtypes = [_vp]
         L.pray_denoiser_gradients.argtypes = [_vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp]
         L.pray_relmse.argtypes = [_vp, ctypes.c_double, _vp, ctypes.c_double, _u64, _vp, _vp]
         for name in EXPORTED:
@@ -394,6 +396,12 @@ class Denoiser:
 
     def __del__(self):
         self.close()
+
+    def set_tensor_cores(self, on: bool) -> None:
+        check(lib().pray_denoiser_set_tensor_cores(self._h, 1 if on else 0))
+
+    def check(self) -> None:
+        check(lib().pray_denoiser_check(self._h))
 
     def get_params(self) -> np.ndarray:
         out = np.empty(self.num_params, np.float32)

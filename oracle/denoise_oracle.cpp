@@ -191,6 +191,8 @@ double orc_unet(const float *params, const float *rad, const uint16_t *feat, con
         low = d[l];
     }
     T y = conv_fwd(d[0], cv[18], params, false);
+    for (size_t p = 0; p < px; p++)
+        for (int k = 0; k < 3; k++) y.v[p * 3 + k] += x0.v[p * 10 + k];  // residual on the input
     // loss
     const size_t nv = px * 3;
     double loss = 0.0;

@@ -86,3 +86,21 @@ def test_features_match_oracle_hits(oracle):
     want[hit, 3:6] = pre[ids[hit], 15:18]
     want[hit, 6] = ts[hit]
     np.testing.assert_array_equal(got, want.astype(np.float16))
+
+
+@pytest.mark.parametrize("shape", [(1, 16, 16), (2, 48, 32)])
+def test_tensor_core_forward_matches_cuda_cores(shape):
+    """The tcgen05 implicit-GEMM convolutions give the CUDA-core result (same
+    BF16 operands, FP32 accumulation; only the summation order differs)."""
+    n, h, w = shape
+    den = native.Denoiser(seed=9)
+    rad, feat, _ = random_batch(4, n, h, w)
+    t = lambda a: torch.from_numpy(a).cuda()
+    outs = []
+    for tc in (False, True):
+        den.set_tensor_cores(tc)
+        out = torch.empty((n, h, w, 3), dtype=torch.float32, device="cuda")
+        den.denoise(t(rad), t(feat), out)
+        den.check()
+        outs.append(out.cpu().numpy())
+    assert rel(np.log1p(outs[1].astype(np.float64)), np.log1p(outs[0].astype(np.float64))) < 5e-3
