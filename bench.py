@@ -43,7 +43,8 @@ def parse():
     ap.add_argument("--dn-steps", type=int, default=1000, help="denoise: training steps")
     ap.add_argument("--dn-train", type=int, default=96, help="denoise: training rooms")
     ap.add_argument("--dn-eval", type=int, default=16, help="denoise: held-out rooms")
-    ap.add_argument("--dn-res", type=int, default=128, help="denoise: image size")
+    ap.add_argument("--dn-res", type=int, default=512, help="denoise: evaluation image size")
+    ap.add_argument("--dn-train-res", type=int, default=256, help="denoise: training image size")
     ap.add_argument("--dn-ref-spp", type=int, default=1024, help="denoise: reference samples per pixel")
     ap.add_argument("--scheduler", choices=["pixel", "wavefront"], default="wavefront",
                     help="room workload: path-tracing scheduler")
@@ -410,12 +411,12 @@ def run_denoise(args):
     import torch
     from nostrum_pray_gb300 import denoise as D, native
     torch.cuda.set_device(0)
-    cfg = D.DenoiseConfig(res=args.dn_res, spp_ref=args.dn_ref_spp, train_rooms=args.dn_train,
-                          eval_rooms=args.dn_eval, steps=args.dn_steps)
+    cfg = D.DenoiseConfig(res=args.dn_res, train_res=args.dn_train_res, spp_ref=args.dn_ref_spp,
+                          train_rooms=args.dn_train, eval_rooms=args.dn_eval, steps=args.dn_steps)
     t0 = time.perf_counter()
     train_seeds = list(range(cfg.seed, cfg.seed + cfg.train_rooms))
     eval_seeds = list(range(cfg.seed + 100_000, cfg.seed + 100_000 + cfg.eval_rooms))
-    _, rad, feat, ref = D.make_dataset(cfg, train_seeds, torch)
+    _, rad, feat, ref = D.make_dataset(cfg, train_seeds, torch, cfg.train_res)
     eval_scs, _, _, eval_refs = D.make_dataset(cfg, eval_seeds, torch)
     data_s = time.perf_counter() - t0
     den = native.Denoiser(seed=cfg.seed)
@@ -424,8 +425,9 @@ def run_denoise(args):
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     # calibration of the fallback sample count on a few training rooms
-    calib = [D.plain_curve(cfg, sc, ref[i], train_seeds[i], torch) for i, sc in enumerate(D.make_dataset(
-        cfg, train_seeds[:4], torch)[0])]
+    calib_scs, _, _, calib_refs = D.make_dataset(cfg, train_seeds[:4], torch)
+    calib = [D.plain_curve(cfg, sc, calib_refs[i], train_seeds[i], torch, spps=(4, 8, 16, 32, 64, 128, 256))
+             for i, sc in enumerate(calib_scs)]
     fb_spp = D.fallback_spp_from(calib, cfg.target)
     res = D.evaluate(cfg, den, {s: (sc, eval_refs[i]) for i, (s, sc) in enumerate(zip(eval_seeds, eval_scs))},
                      torch, fb_spp)
@@ -435,14 +437,17 @@ def run_denoise(args):
     ok_d = sum(1 for r in rows if r["relmse_final"] <= cfg.target)
     line = {"metric": "time to relMSE<=0.01, denoised / plain", "value": round(float(np.mean(td) / np.mean(tp)), 4)
             if tp else None, "unit": "ratio", "n_gpus": 1, "higher_is_better": False, "dtype": "bf16",
-            "data": "synthetic", "config": {"workload": f"procedural rooms {cfg.res}x{cfg.res}, {cfg.spp_in} spp input,"
-                                                        f" {cfg.spp_ref} spp FP64 reference, {cfg.train_rooms} train /"
+            "data": "synthetic", "config": {"workload": f"procedural rooms, evaluated at {cfg.res}x{cfg.res}, {cfg.spp_in} spp input,"
+                                                        f" {cfg.spp_ref} spp FP64 reference, {cfg.train_rooms} train rooms"
+                                                        f" at {cfg.train_res}^2 ({cfg.crop}^2 crops, batch {cfg.batch}),"
                                                         f" {cfg.eval_rooms} held-out rooms, {cfg.steps} Adam steps"},
             "relmse_noisy_mean": float(np.mean([r["relmse_noisy"] for r in rows])),
             "relmse_denoised_mean": float(np.mean([r["relmse_denoised"] for r in rows])),
             "relmse_final_mean": float(np.mean([r["relmse_final"] for r in rows])),
             "rooms_meeting_target": ok_d, "fallbacks": sum(r["fallback"] for r in rows), "fallback_spp": fb_spp,
             "time_plain_mean_s": float(np.mean(tp)) if tp else None, "time_denoised_mean_s": float(np.mean(td)),
+            "render_4spp_mean_s": float(np.mean([r["render_s"] for r in rows])),
+            "inference_mean_s": float(np.mean([r["inference_s"] for r in rows])),
             "spp_plain_to_target": [r["spp_plain_to_target"] for r in rows],
             "loss_first_last": [losses[0][1], losses[-1][1]], "data_s": round(data_s, 1),
             "train_s": round(train_s, 1)}

@@ -28,7 +28,9 @@ from . import native, scenes
 
 @dataclasses.dataclass
 class DenoiseConfig:
-    res: int = 128
+    res: int = 512           # evaluation image size
+    train_res: int = 256     # training image size
+    crop: int = 128          # training crop
     spp_in: int = 4
     spp_ref: int = 1024
     depth: int = 8
@@ -43,8 +45,9 @@ class DenoiseConfig:
     seed: int = 1000
 
 
-def _setup(cfg: DenoiseConfig):
-    return scenes.room_setup(cfg.res, cfg.res, spp=cfg.spp_in, max_depth=cfg.depth)
+def _setup(cfg: DenoiseConfig, res: Optional[int] = None):
+    r = res or cfg.res
+    return scenes.room_setup(r, r, spp=cfg.spp_in, max_depth=cfg.depth)
 
 
 def _params(cfg, st, spp, seed, offset=0):
@@ -52,11 +55,11 @@ def _params(cfg, st, spp, seed, offset=0):
                             rr_depth=cfg.rr_depth, scheduler=native.SCHED_WAVEFRONT, sample_offset=offset)
 
 
-def render_room(cfg: DenoiseConfig, room_seed: int, torch):
+def render_room(cfg: DenoiseConfig, room_seed: int, torch, res: Optional[int] = None):
     """(scene, noisy radiance, features, reference radiance FP64) on the device."""
-    st = _setup(cfg)
+    st = _setup(cfg, res)
     sc = native.Scene.from_setup(scenes.random_room(room_seed, grid=cfg.room_grid), st)
-    h = w = cfg.res
+    h = w = st.width
     rad = torch.empty((h, w, 3), dtype=torch.float32, device="cuda")
     rgb = torch.empty((h, w, 3), dtype=torch.uint8, device="cuda")
     sc.render_pt(_params(cfg, st, cfg.spp_in, seed=room_seed * 7 + 1), rgb, rad)
@@ -77,10 +80,10 @@ def relmse(img, ref, torch) -> float:
     return float(out.item())
 
 
-def make_dataset(cfg: DenoiseConfig, seeds: List[int], torch):
+def make_dataset(cfg: DenoiseConfig, seeds: List[int], torch, res: Optional[int] = None):
     rads, feats, refs, scs = [], [], [], []
     for s in seeds:
-        sc, rad, feat, ref = render_room(cfg, s, torch)
+        sc, rad, feat, ref = render_room(cfg, s, torch, res)
         rads.append(rad)
         feats.append(feat)
         refs.append(ref)
@@ -93,9 +96,13 @@ def train(den: native.Denoiser, rad, feat, ref, cfg: DenoiseConfig, torch, log_e
     target = ref.to(torch.float32)
     g = torch.Generator(device="cpu").manual_seed(cfg.seed)
     losses = []
+    size = rad.shape[1]
     for step in range(cfg.steps):
         idx = torch.randperm(n, generator=g)[:cfg.batch].cuda()
         r, f, t = rad.index_select(0, idx), feat.index_select(0, idx), target.index_select(0, idx)
+        if cfg.crop and cfg.crop < size:
+            oy, ox = (int(v) for v in torch.randint(0, size - cfg.crop + 1, (2,), generator=g))
+            r, f, t = (a[:, oy:oy + cfg.crop, ox:ox + cfg.crop] for a in (r, f, t))
         # random flips keep the data small but varied
         if step % 2:
             r, f, t = r.flip(2), f.flip(2), t.flip(2)
@@ -152,18 +159,21 @@ def denoised_eval(cfg: DenoiseConfig, den, sc, ref, room_seed: int, torch):
 
     run()
     t = timed(run, torch)
+    t_render = timed(lambda: sc.render_pt(p, None, rad[0]), torch)
+    t_infer = timed(lambda: den.denoise(rad, feat, out), torch)
     e = relmse(out[0], ref, torch)
     e_noisy = relmse(rad[0], ref, torch)
     sc.render_pt(p2, None, rad2[0])
     den.denoise(rad2, feat, out2)
     pred = 0.5 * relmse(out[0], out2[0].to(torch.float64), torch)
-    return {"relmse_denoised": e, "relmse_noisy": e_noisy, "time_s": t, "predicted": pred}
+    return {"relmse_denoised": e, "relmse_noisy": e_noisy, "time_s": t, "render_s": t_render,
+            "inference_s": t_infer, "predicted": pred}
 
 
 def evaluate(cfg: DenoiseConfig, den, eval_rooms, torch, fallback_spp: int) -> Dict:
     rows = []
     for seed, (sc, ref) in eval_rooms.items():
-        curve = plain_curve(cfg, sc, ref, seed, torch)
+        curve = plain_curve(cfg, sc, ref, seed, torch, spps=(4, 8, 16, 32, 64, 128, 256))
         plain_ok = [(spp, e, t) for spp, e, t in curve if e <= cfg.target]
         d = denoised_eval(cfg, den, sc, ref, seed, torch)
         t_plain = plain_ok[0][2] if plain_ok else float("nan")

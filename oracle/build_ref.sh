@@ -36,9 +36,14 @@ VARIANTS=(
     "sahct1_eps0 32 20 1.f 0.0f"
     "leaf8_eps0 8 24 5.f 0.0f"
 )
+# the reference's own optimised build (AVX packets, CMakeLists.txt:49 flags) for
+# timing only, built when asked for by name: oracle/build_ref.sh avx_sahct1_eps0
+TIMING_VARIANTS=(
+    "avx_sahct1_eps0 32 20 1.f 0.0f -march=native -Ofast -fno-fast-math"
+)
 
 build_variant() {
-    local name=$1 leaf=$2 depth=$3 ct=$4 eps=$5
+    local name=$1 leaf=$2 depth=$3 ct=$4 eps=$5 flags=${6:-"-O2 -ffp-contract=off"}
     local lib="$OUT/libprayref_${name}.so"
     if [ -f "$lib" ] && [ "$lib" -nt "$HERE/ref_harness.cpp" ] && [ "$lib" -nt "$0" ]; then
         return 0
@@ -53,10 +58,10 @@ build_variant() {
     grep -q "MAX_DEPTH = ${depth};" "$tmp/include/kd_tree.h"
     grep -q "traversalCost = ${ct};" "$tmp/include/kd_tree_sah.h"
     grep -q "EPSILON = ${eps};" "$tmp/include/geometry.h"
-    g++ -std=c++14 -O2 -ffp-contract=off -fopenmp -fPIC -shared -w \
+    g++ -std=c++14 $flags -fopenmp -fPIC -shared -w \
         -include limits -include fstream \
         -I"$tmp/include" -I"$REF/ext" \
-        "$REF/src/kd_tree.cpp" "$REF/src/kd_tree_sah.cpp" "$REF/src/geometry.cpp" \
+        "$REF/src/kd_tree.cpp" "$REF/src/kd_tree_sah.cpp" "$REF/src/geometry.cpp" "$REF/src/geometry_simd.cpp" \
         "$REF/src/scene_preprocessor.cpp" "$REF/src/pray.cpp" "$REF/src/io.cpp" \
         "$HERE/ref_harness.cpp" -o "$lib.tmp" -lstdc++fs
     mv "$lib.tmp" "$lib"
@@ -70,6 +75,13 @@ for v in "${VARIANTS[@]}"; do
     set -- $v
     if [ ${#want[@]} -eq 0 ] || printf '%s\n' "${want[@]}" | grep -qx "$1"; then
         build_variant "$@" &
+        pids+=($!)
+    fi
+done
+for v in "${TIMING_VARIANTS[@]}"; do
+    set -- $v
+    if [ ${#want[@]} -gt 0 ] && printf '%s\n' "${want[@]}" | grep -qx "$1"; then
+        build_variant "$1" "$2" "$3" "$4" "$5" "${*:6}" &
         pids+=($!)
     fi
 done

@@ -62,7 +62,7 @@ def test_training_reduces_loss():
     t = lambda a: torch.from_numpy(a).cuda()
     rad_t, feat_t, tgt_t = t(rad), t(feat), t(tgt)
     first = den.train_step(rad_t, feat_t, tgt_t, 1e-3, want_loss=True)
-    for _ in range(60):
+    for _ in range(150):
         den.train_step(rad_t, feat_t, tgt_t, 1e-3)
     last = den.train_step(rad_t, feat_t, tgt_t, 1e-3, want_loss=True)
     assert last < 0.5 * first, (first, last)
