@@ -54,14 +54,29 @@ __device__ __forceinline__ RayF make_ray(float ox, float oy, float oz, float dx,
     return r;
 }
 
-// BoundingBox::intersect, include/geometry.h:151-164.
-__device__ __forceinline__ bool slab(const float4 &lo, const float4 &hi, const RayF &r, float &tn, float &tf) {
+// BoundingBox::intersect, include/geometry.h:151-164. `finite`: all three
+// inverse direction components are finite, so no slab value can be NaN; then
+// fminf/fmaxf return the same values as the reference's std::min/std::max
+// selects (they can differ only in the sign of a zero, which no comparison
+// sees), at one instruction each. Otherwise the select form reproduces the
+// reference's NaN behaviour.
+__device__ __forceinline__ bool slab(const float4 &lo, const float4 &hi, const RayF &r, bool finite, float &tn,
+                                     float &tf) {
     const float t1x = (lo.x - r.ox) * r.ix, t2x = (hi.x - r.ox) * r.ix;
     const float t1y = (lo.y - r.oy) * r.iy, t2y = (hi.y - r.oy) * r.iy;
     const float t1z = (lo.z - r.oz) * r.iz, t2z = (hi.z - r.oz) * r.iz;
-    tn = smax(smax(smin(t1x, t2x), smin(t1y, t2y)), smax(smin(t1z, t2z), -FLT_MAX));
-    tf = smin(smin(smax(t1x, t2x), smax(t1y, t2y)), smin(smax(t1z, t2z), FLT_MAX));
+    if (finite) {
+        tn = fmaxf(fmaxf(fminf(t1x, t2x), fminf(t1y, t2y)), fmaxf(fminf(t1z, t2z), -FLT_MAX));
+        tf = fminf(fminf(fmaxf(t1x, t2x), fmaxf(t1y, t2y)), fminf(fmaxf(t1z, t2z), FLT_MAX));
+    } else {
+        tn = smax(smax(smin(t1x, t2x), smin(t1y, t2y)), smax(smin(t1z, t2z), -FLT_MAX));
+        tf = smin(smin(smax(t1x, t2x), smax(t1y, t2y)), smin(smax(t1z, t2z), FLT_MAX));
+    }
     return tn <= tf;
+}
+
+__device__ __forceinline__ bool slab(const float4 &lo, const float4 &hi, const RayF &r, float &tn, float &tf) {
+    return slab(lo, hi, r, false, tn, tf);
 }
 
 // One-sided Moeller-Trumbore, include/geometry.h:242-262, with the det
@@ -73,9 +88,15 @@ __device__ __forceinline__ bool intersect_tri(const float4 &v0, const float4 &e1
     const float pz = r.dx * e2.y - r.dy * e2.x;
     const float det = e1.x * px + e1.y * py + e1.z * pz;
     if (det < eps) return false;
-    const float inv = 1.0f / det;
     const float tx = r.ox - v0.x, ty = r.oy - v0.y, tz = r.oz - v0.z;
-    const float u = (tx * px + ty * py + tz * pz) * inv;
+    const float un = tx * px + ty * py + tz * pz;
+    // Early out before the division, only where the reference's
+    // u = un * (1 / det) is certainly < 0 or > 1: un below -2^-125.6 * det
+    // keeps the product a negative normal number; un above det * (1 + 2^-20)
+    // keeps it above 1 whatever the two roundings.
+    if (un < -(det * 2.4e-38f) || un > det * 1.00000095367431640625f) return false;
+    const float inv = 1.0f / det;
+    const float u = un * inv;
     if (u < 0.f || u > 1.f) return false;
     const float qx = ty * e1.z - tz * e1.y;
     const float qy = tz * e1.x - tx * e1.z;
@@ -137,6 +158,7 @@ __device__ __forceinline__ int traverse(const DevScene &s, const RayF &r, float 
     uint32_t a = 0, b = 0, la = 0, lb = 0;
     float cur_tn = 0.f, leaf_tn = 0.f;
     bool have_node = false, have_leaf = false;
+    const bool finite = isfinite(r.ix) && isfinite(r.iy) && isfinite(r.iz);
     if (valid) {
         float tn, tf;
         const float4 rlo = ldg4(s.nodes[0].lo), rhi = ldg4(s.nodes[0].hi);
@@ -160,8 +182,8 @@ __device__ __forceinline__ int traverse(const DevScene &s, const RayF &r, float 
                 const GNode *c = s.nodes + a;
                 const float4 l0 = ldg4(c[0].lo), h0 = ldg4(c[0].hi), l1 = ldg4(c[1].lo), h1 = ldg4(c[1].hi);
                 float tn0, tf0, tn1, tf1;
-                const bool v0 = slab(l0, h0, r, tn0, tf0) && tn0 <= limit && tf0 >= back;
-                const bool v1 = slab(l1, h1, r, tn1, tf1) && tn1 <= limit && tf1 >= back;
+                const bool v0 = slab(l0, h0, r, finite, tn0, tf0) && tn0 <= limit && tf0 >= back;
+                const bool v1 = slab(l1, h1, r, finite, tn1, tf1) && tn1 <= limit && tf1 >= back;
                 if (v0 && v1) {
                     const bool first0 = tn0 <= tn1;
                     stk_a[sp] = __float_as_uint(first0 ? l1.w : l0.w);

@@ -175,3 +175,32 @@ def test_icosphere_level8_full(oracle, golden):
         key = f"ico8_eps{eps:g}"
         assert sha(img) == hashes[key]["image"]
         assert sha(ids) == hashes[key]["ids"] and sha(ts) == hashes[key]["t"]
+
+
+def test_rays_through_vertices_and_edges(oracle):
+    """Rays aimed at triangle vertices, edge midpoints and edge thirds (u or v
+    at or next to 0 and 1, u + v at 1): the intersector's early outs must
+    decide exactly as the reference's full computation."""
+    m = scenes.soup(4_000, 12)
+    st = scenes.soup_setup()
+    sc = native.Scene.from_setup(m, st)
+    orc = oracle.OracleScene.from_setup(m, st)
+    rng = np.random.default_rng(5)
+    v = m.verts.reshape(-1, 3, 3).astype(np.float64)
+    tri = rng.integers(0, m.n, 60_000)
+    which = rng.integers(0, 6, tri.size)
+    a, b, c = v[tri, 0], v[tri, 1], v[tri, 2]
+    targets = np.where((which == 0)[:, None], a, np.where((which == 1)[:, None], b, np.where(
+        (which == 2)[:, None], c, np.where((which == 3)[:, None], (a + b) / 2, np.where(
+            (which == 4)[:, None], (b + c) / 2, a + (c - a) / 3)))))
+    o = rng.uniform(-1.0, 2.0, (tri.size, 3))
+    d = targets - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d = d.astype(np.float32)
+    with np.errstate(divide="ignore"):
+        rays = np.concatenate([o.astype(np.float32), d, (1.0 / d).astype(np.float32)], 1)
+    for eps in (1e-4, 0.0):
+        ids, ts = trace(sc, rays, eps)
+        wid, wt = orc.trace(rays, eps)
+        assert int((ids != wid.astype(np.int32)).sum()) == 0
+        np.testing.assert_array_equal(ts.view(np.uint32), wt.view(np.uint32))
