@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--dn-train", type=int, default=96, help="denoise: training rooms")
     ap.add_argument("--dn-eval", type=int, default=16, help="denoise: held-out rooms")
     ap.add_argument("--dn-res", type=int, default=512, help="denoise: evaluation image size")
-    ap.add_argument("--dn-train-res", type=int, default=256, help="denoise: training image size")
+    ap.add_argument("--dn-train-res", type=int, default=512, help="denoise: training image size")
     ap.add_argument("--dn-ref-spp", type=int, default=1024, help="denoise: reference samples per pixel")
     ap.add_argument("--scheduler", choices=["pixel", "wavefront"], default="wavefront",
                     help="room workload: path-tracing scheduler")
