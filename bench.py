@@ -39,12 +39,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["icosphere", "soup", "room", "batch", "denoise"], default="icosphere")
+    ap.add_argument("--workload", choices=["icosphere", "soup", "room", "batch", "denoise", "denoise-infer"], default="icosphere")
     ap.add_argument("--dn-steps", type=int, default=1000, help="denoise: training steps")
     ap.add_argument("--dn-train", type=int, default=96, help="denoise: training rooms")
     ap.add_argument("--dn-eval", type=int, default=16, help="denoise: held-out rooms")
     ap.add_argument("--dn-res", type=int, default=512, help="denoise: evaluation image size")
     ap.add_argument("--dn-train-res", type=int, default=512, help="denoise: training image size")
+    ap.add_argument("--dn-cuda-cores", action="store_true", help="denoise-infer: CUDA-core convolutions")
     ap.add_argument("--dn-ref-spp", type=int, default=1024, help="denoise: reference samples per pixel")
     ap.add_argument("--scheduler", choices=["pixel", "wavefront"], default="wavefront",
                     help="room workload: path-tracing scheduler")
@@ -138,6 +139,14 @@ def measured_peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def measured_bf16():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured cuBLAS bf16 (burst)"
+    return 1900.0, "fallback cuBLAS bf16 (burst)"
 
 
 def committed_traffic(kernel: str, workload_name: str):
@@ -454,6 +463,67 @@ def run_denoise(args):
     print(json.dumps(line), flush=True)
 
 
+def run_denoise_infer(args):
+    """Denoiser inference on one 512x512 frame (a 4-spp render of a
+    procedural room and its features), the tensor-core forward pass."""
+    import torch
+    from nostrum_pray_gb300 import denoise as D, native
+    torch.cuda.set_device(0)
+    res = args.dn_res
+    cfg = D.DenoiseConfig(res=res, spp_ref=1)
+    st = D._setup(cfg)
+    sc = native.Scene.from_setup(D.scenes.random_room(cfg.seed, grid=cfg.room_grid), st)
+    rad = torch.empty((1, res, res, 3), dtype=torch.float32, device="cuda")
+    feat = torch.empty((1, res, res, 7), dtype=torch.float16, device="cuda")
+    sc.render_pt(D._params(cfg, st, cfg.spp_in, seed=1), None, rad[0])
+    sc.render_features(D._params(cfg, st, 1, seed=0), feat[0])
+    out = torch.empty_like(rad)
+    den = native.Denoiser(seed=cfg.seed)
+    if args.dn_cuda_cores:
+        den.set_tensor_cores(False)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    clocks = ClockSampler(0)
+    clocks.start()
+    ms = _timed_frames(lambda: den.denoise(rad, feat, out), args.steps, args.warmup, flush)
+    clk = clocks.stop()
+    den.check()
+    # end to end: pinned host input -> device, inference, output -> pinned host
+    h_rad, h_feat = rad.cpu().pin_memory(), feat.cpu().pin_memory()
+    h_out = torch.empty(out.shape, dtype=out.dtype).pin_memory()
+    stream = torch.cuda.current_stream()
+
+    def e2e_step():
+        rad.copy_(h_rad, non_blocking=True)
+        feat.copy_(h_feat, non_blocking=True)
+        den.denoise(rad, feat, out)
+        h_out.copy_(out, non_blocking=True)
+
+    e2e_ms = _timed_frames(e2e_step, args.steps, args.warmup, flush)
+    stream.synchronize()
+    flops = D.forward_flops(res, res)
+    per = ms / args.steps / 1e3
+    peak, peak_kind = measured_bf16()
+    achieved = flops / per / 1e12
+    line = {"metric": "denoised frames/s", "value": round(args.steps / (ms / 1e3), 2), "unit": "frames/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": f"U-Net denoiser inference (19 3x3 convs, {D.num_params()} parameters, random "
+                                   f"initialisation), one {res}x{res} frame: 4-spp room render + features",
+                       "tensor_cores": not args.dn_cuda_cores, "l2": "flushed between steps"},
+            "e2e": {"value": round(args.steps / (e2e_ms / 1e3), 2), "unit": "frames/s",
+                    "h2d_bytes_per_step": rad.numel() * 4 + feat.numel() * 2, "d2h_bytes_per_step": out.numel() * 4},
+            # per frame: input packing, 19 convolutions, 4 pools, 4 upsamplings, 4 concatenations,
+            # residual add, output transform
+            "gpu_launches": 34 * args.steps,
+            "roofline": {"bound": "tensor", "achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s",
+                         "frac": round(achieved / peak, 5), "traffic": None, "peak_kind": peak_kind,
+                         "algorithmic_flops_per_frame": flops,
+                         "note": "whole forward pass timed (convolutions plus pooling, upsampling, concatenation"
+                                 " and packing kernels)"},
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -464,6 +534,8 @@ def main():
         run_batch(args)
     elif args.workload == "denoise":
         run_denoise(args)
+    elif args.workload == "denoise-infer":
+        run_denoise_infer(args)
     else:
         run_ours(args)
 

@@ -47,6 +47,22 @@ class DenoiseConfig:
     seed: int = 1000
 
 
+# (cin, cout, level) of the network's 19 3x3 convolutions in forward order
+# (the table of csrc/denoise_net.cpp; level l runs at (h >> l) x (w >> l))
+CONVS = [(10, 32, 0), (32, 32, 0), (32, 48, 1), (48, 48, 1), (48, 64, 2), (64, 64, 2), (64, 96, 3), (96, 96, 3),
+         (96, 128, 4), (128, 128, 4), (224, 96, 3), (96, 96, 3), (160, 64, 2), (64, 64, 2), (112, 48, 1),
+         (48, 48, 1), (80, 32, 0), (32, 32, 0), (32, 3, 0)]
+
+
+def num_params() -> int:
+    return sum(9 * ci * co + co for ci, co, _ in CONVS)
+
+
+def forward_flops(h: int, w: int, n: int = 1) -> int:
+    """Multiply-add FLOPs (2 per MAC) of the convolutions of one forward pass."""
+    return n * sum(2 * 9 * ci * co * (h >> l) * (w >> l) for ci, co, l in CONVS)
+
+
 def _setup(cfg: DenoiseConfig, res: Optional[int] = None):
     r = res or cfg.res
     return scenes.room_setup(r, r, spp=cfg.spp_in, max_depth=cfg.depth)

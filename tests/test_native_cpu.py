@@ -154,3 +154,11 @@ def test_device_layout_valid(refine):
             assert refined == 0 and added == 0 and nodes == int(st_[0]) + 1
         else:
             assert nodes == int(st_[0]) + 1 + added
+
+
+def test_denoiser_table_matches_oracle(oracle):
+    """The conv table used for FLOP counts has the oracle network's parameter
+    count; 47.6 GFLOP per 512x512 forward."""
+    from nostrum_pray_gb300 import denoise
+    assert denoise.num_params() == int(oracle.lib().orc_unet_num_params()) == 1_016_419
+    assert denoise.forward_flops(512, 512) == 47_563_407_360
