@@ -74,7 +74,13 @@ typedef struct {
  * src/io.cpp:60-63). */
 typedef enum {
     PRAY_PT_KAJIYA = 0,   /* the reference's evaluatePathRecursive (src/pray.cpp:342-364) */
-    PRAY_PT_NEE = 1       /* next-event estimation + Russian roulette (no reference counterpart) */
+    PRAY_PT_NEE = 1,      /* next-event estimation + Russian roulette (no reference counterpart) */
+    PRAY_PT_DIFFUSE = 2   /* the reference's branching evaluatePathRecursiveDiffuse (src/pray.cpp:315-340,
+                             src/path_trace.cu:369-393): every non-emitting hit above max_depth spawns
+                             num_samples bounce rays and returns albedo x their mean, so a pixel casts up to
+                             1 + n + ... + n^max_depth rays; one estimate per pixel from the PCG32 stream
+                             (seed, pixel, sample_offset); max_depth <= 8; PRAY_SCHED_PIXEL only. The
+                             reference selects it when max_depth <= 1 (src/scene_preprocessor.cpp:34-40) */
 } pray_pt_mode;
 
 typedef enum {
@@ -90,7 +96,7 @@ typedef struct {
     float camera_look[3];
     float background[3];
     uint32_t max_depth;            /* bounces: a hit at depth >= max_depth returns 0 */
-    uint32_t num_samples;          /* paths per pixel */
+    uint32_t num_samples;          /* paths per pixel (PRAY_PT_DIFFUSE: bounce rays per hit) */
     uint64_t seed;                 /* PCG32 streams per (seed, pixel, sample) */
     float det_epsilon;
     int32_t mode;                  /* pray_pt_mode */
@@ -192,7 +198,8 @@ pray_status pray_render_pt_host(pray_scene *s, const pray_pt_params *p, uint8_t 
  * [sample_offset, sample_offset + num_samples) of every pixel to sum_dev
  * (height x width x 3 doubles, caller-initialised), one sample at a time in
  * sample order, so repeated calls over consecutive sample ranges give the
- * same sums as one call. Device pointers; enqueued on `stream`. */
+ * same sums as one call. Device pointers; enqueued on `stream`. Not for
+ * PRAY_PT_DIFFUSE (PRAY_ERR_UNSUPPORTED). */
 pray_status pray_accumulate_pt(pray_scene *s, const pray_pt_params *p, double *sum_dev,
                                unsigned long long *counters_dev, void *stream);
 
@@ -229,7 +236,8 @@ typedef struct {
 } pray_batch_config;
 
 /* Records n scenes (all on one device) with one path-tracing frame each:
- * params[i] as for pray_render_pt (scheduler and wavefront_paths ignored),
+ * params[i] as for pray_render_pt (scheduler and wavefront_paths ignored;
+ * PRAY_PT_KAJIYA or PRAY_PT_NEE),
  * rgb_dev[i] / radiance_dev[i] its outputs (device pointers; each may be
  * NULL, not both). The scenes must outlive the batch. */
 pray_status pray_batch_create(pray_scene *const *scenes, const pray_pt_params *params, uint8_t *const *rgb_dev,

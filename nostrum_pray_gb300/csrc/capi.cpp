@@ -202,8 +202,10 @@ pray_status check_pt_params(const pray_pt_params *p) {
     if (p->num_samples == 0) return set_error(PRAY_ERR_INVALID_ARGUMENT, "num_samples must be >= 1");
     if (p->max_depth >= (uint32_t)kMaxPtDepth)
         return set_error(PRAY_ERR_UNSUPPORTED, "max_depth must be below 64");
-    if (p->mode != PRAY_PT_KAJIYA && p->mode != PRAY_PT_NEE)
-        return set_error(PRAY_ERR_INVALID_ARGUMENT, "mode must be PRAY_PT_KAJIYA or PRAY_PT_NEE");
+    if (p->mode != PRAY_PT_KAJIYA && p->mode != PRAY_PT_NEE && p->mode != PRAY_PT_DIFFUSE)
+        return set_error(PRAY_ERR_INVALID_ARGUMENT, "mode must be PRAY_PT_KAJIYA, PRAY_PT_NEE or PRAY_PT_DIFFUSE");
+    if (p->mode == PRAY_PT_DIFFUSE && p->max_depth > (uint32_t)kMaxDiffuseDepth)
+        return set_error(PRAY_ERR_UNSUPPORTED, "PRAY_PT_DIFFUSE: max_depth must be at most 8");
     if (p->scheduler != PRAY_SCHED_PIXEL && p->scheduler != PRAY_SCHED_WAVEFRONT)
         return set_error(PRAY_ERR_INVALID_ARGUMENT, "scheduler must be PRAY_SCHED_PIXEL or PRAY_SCHED_WAVEFRONT");
     if (p->scheduler == PRAY_SCHED_WAVEFRONT && p->mode != PRAY_PT_NEE)
@@ -637,6 +639,8 @@ pray_status pray_accumulate_pt(pray_scene *s, const pray_pt_params *p, double *s
     if (!s || !sum) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
     pray_status st = check_pt_params(p);
     if (st != PRAY_OK) return st;
+    if (p->mode == PRAY_PT_DIFFUSE)
+        return set_error(PRAY_ERR_UNSUPPORTED, "PRAY_PT_DIFFUSE makes one estimate per pixel; nothing to accumulate");
     cudaError_t e = cudaSetDevice(s->device);
     if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
     PtLaunch L = make_pt_launch(p);
@@ -772,6 +776,8 @@ pray_status pray_batch_create(pray_scene *const *scenes, const pray_pt_params *p
         p.scheduler = PRAY_SCHED_PIXEL;
         pray_status st = check_pt_params(&p);
         if (st != PRAY_OK) return st;
+        if (p.mode == PRAY_PT_DIFFUSE)
+            return set_error(PRAY_ERR_UNSUPPORTED, "batches run PRAY_PT_KAJIYA or PRAY_PT_NEE");
         uint8_t *o8 = rgb ? rgb[i] : nullptr;
         float *of = radiance ? radiance[i] : nullptr;
         if (!o8 && !of) return set_error(PRAY_ERR_INVALID_ARGUMENT, "batch item without an output");

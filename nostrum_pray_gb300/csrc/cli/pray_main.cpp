@@ -110,6 +110,15 @@ int main(int argc, char **argv) {
         }
         p.max_depth = (uint32_t)scene.max_depth;
         p.num_samples = (uint32_t)scene.num_samples;
+        // the reference's mode choice (src/scene_preprocessor.cpp:34-40, MAX_DEPTH_DIFFUSE = 1 in
+        // include/options.h:32): branching up to depth 1, one bounce per sample above it
+        if (scene.max_depth > 1) {
+            std::printf("\tUsing normal path tracing.\n");
+            p.mode = PRAY_PT_KAJIYA;
+        } else {
+            std::printf("\tUsing diffuse path tracing.\n");
+            p.mode = PRAY_PT_DIFFUSE;
+        }
         p.seed = scene.seed;
         p.det_epsilon = scene.det_epsilon;
         rc = pray_render_pt_host(s, &p, image.data(), nullptr, nullptr);

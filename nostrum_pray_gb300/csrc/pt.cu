@@ -1,5 +1,6 @@
-// Per-pixel path-tracing kernel: one lane per pixel (pt_pixel.cuh), warps
-// over 8x4 pixel tiles. Built with --fmad=false like the rest of the
+// Per-pixel path-tracing kernels: one lane per pixel (pt_pixel.cuh), warps
+// over 8x4 pixel tiles; the branching mode has a kernel of its own so that its
+// frame stack does not weigh on the other modes. Built with --fmad=false like the rest of the
 // tracing code.
 #include <cstdint>
 
@@ -22,6 +23,15 @@ __global__ void __launch_bounds__(128) k_render_pt(DevScene s, PtLaunch L) {
     if (L.counters) count_paths(L.counters, active, L.num_samples, segments);
 }
 
+__global__ void __launch_bounds__(128) k_render_pt_diffuse(DevScene s, PtLaunch L) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t px, py;
+    const bool active = pixel_of(i, L.cam.width, L.cam.height, px, py);
+    uint32_t segments = 0;
+    pt_pixel_diffuse<kStack>(s, L, active, px, py, segments);
+    if (L.counters) count_paths(L.counters, active, 1, segments);
+}
+
 }  // namespace
 
 cudaError_t launch_render_pt(const DevScene &s, const PtLaunch &L, cudaStream_t stream) {
@@ -29,7 +39,10 @@ cudaError_t launch_render_pt(const DevScene &s, const PtLaunch &L, cudaStream_t 
     const uint64_t threads = tiles * 32;
     if (threads == 0) return cudaSuccess;
     const unsigned bs = 128;
-    k_render_pt<<<(unsigned)((threads + bs - 1) / bs), bs, 0, stream>>>(s, L);
+    if (L.mode == 2)
+        k_render_pt_diffuse<<<(unsigned)((threads + bs - 1) / bs), bs, 0, stream>>>(s, L);
+    else
+        k_render_pt<<<(unsigned)((threads + bs - 1) / bs), bs, 0, stream>>>(s, L);
     return cudaGetLastError();
 }
 

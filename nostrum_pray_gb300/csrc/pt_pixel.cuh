@@ -16,6 +16,8 @@
 // emitting triangles (area-weighted choice, uniform point, one occlusion ray)
 // and Russian roulette from rr_depth; emitters seen by a bounce ray end the
 // path without adding their emission (next-event estimation accounts for it).
+//
+// Mode 2 (pt_pixel_diffuse below) is the reference's branching variant.
 #pragma once
 
 #include <cfloat>
@@ -182,6 +184,94 @@ __device__ __forceinline__ void pt_pixel(const DevScene &s, const PtLaunch &L, b
             o[0] = (uint8_t)quantise(smax(0.f, smin(1.f, mr)));
             o[1] = (uint8_t)quantise(smax(0.f, smin(1.f, mg)));
             o[2] = (uint8_t)quantise(smax(0.f, smin(1.f, mb)));
+        }
+    }
+}
+
+// Mode 2 restates the reference's branching recursion
+// (evaluatePathRecursiveDiffuse, src/pray.cpp:315-340; its GPU twin
+// src/path_trace.cu:369-393): a miss returns the background, an emitter its
+// colour, a hit at depth >= max_depth black; any other hit casts num_samples
+// cosine bounce rays one after another and returns (sum * albedo) /
+// num_samples. The recursion is unrolled into a per-lane stack of frames (one
+// per ancestor hit: position, normal, albedo, running sum, children done); a
+// finished ray's value is folded into its parent frame, and every frame whose
+// children are all done is folded into its own parent in turn. One PCG32
+// stream per pixel (sample index sample_offset) supplies the two uniforms of
+// each bounce in depth-first order. As in pt_pixel, every lane of a warp
+// iterates until the warp's last tree ends, so the traversals line up.
+template <int kStackN>
+__device__ __forceinline__ void pt_pixel_diffuse(const DevScene &s, const PtLaunch &L, bool active, uint32_t px,
+                                                 uint32_t py, uint32_t &segments) {
+    constexpr unsigned kFull = 0xFFFFFFFFu;
+    const uint64_t pixel = active ? (uint64_t)py * L.cam.width + px : 0;
+    RayF r = primary_ray(L.cam, active ? px : 0, active ? py : 0);
+    pray_pcg32 rng = pray_pcg32_stream(L.seed, pixel, L.sample_offset);
+    float fpos[kMaxDiffuseDepth][3], fnrm[kMaxDiffuseDepth][3], falb[kMaxDiffuseDepth][3],
+        fsum[kMaxDiffuseDepth][3];
+    uint32_t fdone[kMaxDiffuseDepth];
+    uint32_t top = 0;  // frames on the stack = depth of the ray in flight
+    float res0 = 0.f, res1 = 0.f, res2 = 0.f;
+    bool alive = active;
+    const bool any_geometry = s.n_refs > 0;
+    const float nf = (float)L.num_samples;
+    while (__any_sync(kFull, alive)) {
+        float t;
+        const int pos = traverse<false, false, kStackN>(s, r, L.eps, 0.f, alive && any_geometry, t);
+        if (alive) {
+            segments++;
+            bool ends = true;
+            float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+            if (pos < 0) {
+                v0 = L.bg[0], v1 = L.bg[1], v2 = L.bg[2];
+            } else {
+                const int id = (int)__float_as_uint(__ldg(&s.tris[pos].v0[3]));
+                const float4 nrm = shade_n(s, id), col = shade_c(s, id);
+                if (nrm.w != 0.f) {
+                    v0 = col.x, v1 = col.y, v2 = col.z;
+                } else if (top < L.max_depth) {
+                    fpos[top][0] = r.ox + r.dx * t, fpos[top][1] = r.oy + r.dy * t, fpos[top][2] = r.oz + r.dz * t;
+                    fnrm[top][0] = nrm.x, fnrm[top][1] = nrm.y, fnrm[top][2] = nrm.z;
+                    falb[top][0] = col.x, falb[top][1] = col.y, falb[top][2] = col.z;
+                    fsum[top][0] = 0.f, fsum[top][1] = 0.f, fsum[top][2] = 0.f;
+                    fdone[top] = 0;
+                    top++;
+                    ends = false;
+                }
+            }
+            while (ends) {
+                if (top == 0) {
+                    res0 = v0, res1 = v1, res2 = v2;
+                    alive = false;
+                    break;
+                }
+                const uint32_t k = top - 1;
+                fsum[k][0] = fsum[k][0] + v0, fsum[k][1] = fsum[k][1] + v1, fsum[k][2] = fsum[k][2] + v2;
+                if (++fdone[k] < L.num_samples) break;
+                v0 = (fsum[k][0] * falb[k][0]) / nf;
+                v1 = (fsum[k][1] * falb[k][1]) / nf;
+                v2 = (fsum[k][2] * falb[k][2]) / nf;
+                top = k;
+            }
+            if (alive) {
+                const uint32_t k = top - 1;
+                const float u1 = pray_uniform(&rng), u2 = pray_uniform(&rng);
+                float d[3];
+                pray_sample_hemisphere(fnrm[k], u1, u2, d);
+                r = make_ray(fpos[k][0], fpos[k][1], fpos[k][2], d[0], d[1], d[2]);
+            }
+        }
+    }
+    if (active) {
+        if (L.radiance) {
+            float *o = L.radiance + 3 * pixel;
+            o[0] = res0, o[1] = res1, o[2] = res2;
+        }
+        if (L.rgb) {
+            uint8_t *o = L.rgb + 3 * pixel;
+            o[0] = (uint8_t)quantise(smax(0.f, smin(1.f, res0)));
+            o[1] = (uint8_t)quantise(smax(0.f, smin(1.f, res1)));
+            o[2] = (uint8_t)quantise(smax(0.f, smin(1.f, res2)));
         }
     }
 }

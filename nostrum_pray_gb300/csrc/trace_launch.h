@@ -30,12 +30,13 @@ struct RtLaunch {
 };
 
 constexpr int kMaxPtDepth = 64;  // bounce limit of the path tracer (per-thread albedo stack)
+constexpr int kMaxDiffuseDepth = 8;  // depth limit of the branching mode (per-thread frame stack)
 
 struct PtLaunch {
     CameraConsts cam;
     float bg[3];
     uint32_t max_depth, num_samples, rr_depth;
-    int32_t mode;                    // 0: reference recursion, 1: NEE + Russian roulette
+    int32_t mode;                    // 0: reference recursion, 1: NEE + Russian roulette, 2: branching
     uint64_t seed;
     float eps;
     uint32_t sample_offset;          // first sample index (PCG stream selector)

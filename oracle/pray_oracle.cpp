@@ -515,7 +515,8 @@ inline uint8_t quantise(float c) {
 // (src/pray.cpp:342-378) with the PCG32 streams and hemisphere sampling of
 // include/nostrum_pray_sampling.h in place of the reference's clock-seeded
 // mt19937_64. NEE mode is this project's next-event-estimation variant (no
-// reference counterpart); the CUDA kernel must match this code's float
+// reference counterpart); branching mode restates the reference's
+// evaluatePathRecursiveDiffuse. The CUDA kernels must match this code's float
 // operation order.
 
 struct Emitters {
@@ -571,6 +572,34 @@ V3 path_kajiya(const Scene &s, Ray r, V3 bg, uint32_t max_depth, float eps, pray
     }
     for (size_t k = albedo.size(); k-- > 0;) L = mul(L, albedo[k]);
     return L;
+}
+
+// The reference's branching recursion (evaluatePathRecursiveDiffuse,
+// src/pray.cpp:315-340): num_samples bounce rays at every non-emitting hit
+// above max_depth, (sum of their values * albedo) / num_samples. The two
+// uniforms of each bounce come from one PCG32 stream in depth-first order
+// (the reference draws from a clock-seeded mt19937_64 per call).
+V3 path_diffuse(const Scene &s, const Ray &r, V3 bg, uint32_t max_depth, uint32_t n, float eps, pray_pcg32 &g,
+                uint64_t &segs, uint32_t depth) {
+    int64_t id;
+    float t;
+    segs++;
+    if (!closest(s, r, eps, id, t)) return bg;
+    const Tri &tri = s.tris[id];
+    if (tri.emit) return tri.color;
+    if (depth >= max_depth) return {0.f, 0.f, 0.f};
+    const V3 hit = add(r.o, scale(r.d, t));
+    const float nrm[3] = {tri.normal.x, tri.normal.y, tri.normal.z};
+    V3 sum{0.f, 0.f, 0.f};
+    for (uint32_t i = 0; i < n; i++) {
+        const float u1 = pray_uniform(&g), u2 = pray_uniform(&g);
+        float d[3];
+        pray_sample_hemisphere(nrm, u1, u2, d);
+        sum = add(sum, path_diffuse(s, make_ray(hit, {d[0], d[1], d[2]}), bg, max_depth, n, eps, g, segs, depth + 1));
+    }
+    const V3 m = mul(sum, tri.color);
+    const float nf = (float)n;
+    return {m.x / nf, m.y / nf, m.z / nf};
 }
 
 V3 path_nee(const Scene &s, const Emitters &em, Ray r, V3 bg, uint32_t max_depth, uint32_t rr_depth, float eps,
@@ -675,7 +704,14 @@ uint64_t orc_render_pt(void *h, uint64_t w, uint64_t hh, uint64_t fov, const flo
             V3 sum{0.f, 0.f, 0.f};
             const uint64_t o = (py - row0) * w + px;
             double *acc = out_sum64 ? out_sum64 + 3 * o : nullptr;
-            for (uint32_t k = 0; k < spp; k++) {
+            if (mode == 2) {
+                // branching mode: one tree per pixel, spp = bounce rays per hit (evaluatePath,
+                // src/pray.cpp:366-378, returns the tree's value without a further average)
+                pray_pcg32 g = pray_pcg32_stream(seed, pixel, sample_offset);
+                sum = path_diffuse(s, prim, b, max_depth, spp, eps, g, segs, 0);
+                if (acc) acc[0] += (double)sum.x, acc[1] += (double)sum.y, acc[2] += (double)sum.z;
+            }
+            for (uint32_t k = 0; k < (mode == 2 ? 0u : spp); k++) {
                 pray_pcg32 g = pray_pcg32_stream(seed, pixel, sample_offset + k);
                 const V3 L = mode == 0 ? path_kajiya(s, prim, b, max_depth, eps, g, segs)
                                        : path_nee(s, em, prim, b, max_depth, rr_depth, eps, g, segs);
@@ -683,7 +719,7 @@ uint64_t orc_render_pt(void *h, uint64_t w, uint64_t hh, uint64_t fov, const flo
                 if (acc) acc[0] += (double)L.x, acc[1] += (double)L.y, acc[2] += (double)L.z;
             }
             const float ns = (float)spp;
-            const V3 mean{sum.x / ns, sum.y / ns, sum.z / ns};
+            const V3 mean = mode == 2 ? sum : V3{sum.x / ns, sum.y / ns, sum.z / ns};
             if (out_rad) {
                 out_rad[3 * o] = mean.x;
                 out_rad[3 * o + 1] = mean.y;

@@ -129,3 +129,31 @@ def test_oracle_detects_planted_mistake(oracle):
     m.verts[k, 0::3] = np.nextafter(m.verts[k, 0::3].max(), np.float32(2))
     b = dump_hash(oracle.OracleScene.from_setup(m, st).tree_dump())
     assert a != b
+
+
+@pytest.mark.parametrize("depth,n", [(0, 4), (1, 4), (1, 3), (2, 3)])
+def test_oracle_branching_known_answer(oracle, depth, n):
+    """The branching path tracer (evaluatePathRecursiveDiffuse,
+    src/pray.cpp:315-340) on one front-facing triangle: bounce rays leave
+    through its front side and are culled by the one-sided test, so every
+    bounce returns the background and a covered pixel is exactly
+    (bg + ... + bg) * albedo / n at depth >= 1 (black at depth 0); other
+    pixels show the background. Rays: one per pixel plus n per covered pixel."""
+    m = scenes.Mesh(np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32), np.array([[0.5, 0.25, 0.75]], np.float32),
+                    np.zeros(1, np.uint8))
+    st = scenes.RenderSetup(width=24, height=20, fov=60, cam_pos=(0.25, 0.25, 2.0), cam_look=(0, 0, -1), lights=[],
+                            background=(0.5, 0.5, 0.5))
+    osc = oracle.OracleScene.from_setup(m, st)
+    rays = oracle.primary_rays(st.width, st.height, st.fov, st.cam_pos, st.cam_look)
+    ids, _ = osc.trace(rays, st.det_eps)
+    covered = (ids >= 0).reshape(st.height, st.width)
+    assert 0 < covered.sum() < covered.size
+    img, rad, segs = osc.render_pt(st, spp=n, max_depth=depth, seed=1, mode=2)
+    bg = np.float32(0.5)
+    s = np.float32(0)
+    for _ in range(n):
+        s = np.float32(s + bg)
+    hit = (s * m.colors[0]) / np.float32(n) if depth >= 1 else np.zeros(3, np.float32)
+    want = np.where(covered[..., None], hit[None, None, :], np.full(3, bg, np.float32)).astype(np.float32)
+    np.testing.assert_array_equal(rad, want)
+    assert segs == covered.size + (n * int(covered.sum()) if depth >= 1 else 0)

@@ -132,3 +132,42 @@ def test_relmse_reduction():
     native.relmse(ta, 0.5, tr, 2.0, out)
     torch.cuda.synchronize()
     assert abs(out.item() - want) <= 1e-12 * max(1.0, want)
+
+
+@pytest.mark.parametrize("depth,n", [(0, 4), (1, 8), (2, 5)])
+def test_diffuse_branching_room(oracle, depth, n):
+    """The reference's branching mode (evaluatePathRecursiveDiffuse): n bounce
+    rays at every hit above max_depth, one estimate per pixel."""
+    m = scenes.room(grid=6)
+    st = scenes.room_setup(40, 32)
+    sc = native.Scene.from_setup(m, st)
+    orc = oracle.OracleScene.from_setup(m, st)
+    for off in (0, 3):
+        p = native.pt_params(st, spp=n, max_depth=depth, seed=7, mode=native.PT_DIFFUSE, sample_offset=off)
+        img, rad, cnt = sc.render_pt_host(p)
+        oimg, orad, osegs = orc.render_pt(st, spp=n, max_depth=depth, seed=7, mode=native.PT_DIFFUSE,
+                                          sample_offset=off)
+        bad = ~np.isclose(rad, orad, rtol=RTOL, atol=ATOL)
+        assert int(bad.sum()) == 0, f"{int(bad.sum())} radiance values differ"
+        assert int(cnt[0]) == st.width * st.height
+        assert int(cnt[1]) == osegs
+        np.testing.assert_array_equal(img, oimg)
+    # rays per pixel can reach 1 + n + ... + n^depth
+    assert osegs <= st.width * st.height * sum(n ** k for k in range(depth + 1))
+
+
+def test_diffuse_mode_limits():
+    m = scenes.room(grid=3)
+    st = scenes.room_setup(16, 16)
+    sc = native.Scene.from_setup(m, st)
+    with pytest.raises(native.PrayError):
+        sc.render_pt_host(native.pt_params(st, spp=2, max_depth=9, mode=native.PT_DIFFUSE))
+    with pytest.raises(native.PrayError):
+        sc.render_pt_host(native.pt_params(st, spp=2, max_depth=1, mode=native.PT_DIFFUSE,
+                                           scheduler=native.SCHED_WAVEFRONT))
+    acc = torch.zeros((16, 16, 3), dtype=torch.float64, device="cuda")
+    with pytest.raises(native.PrayError):
+        sc.accumulate_pt(native.pt_params(st, spp=2, max_depth=1, mode=native.PT_DIFFUSE), acc)
+    rgb = torch.empty((16, 16, 3), dtype=torch.uint8, device="cuda")
+    with pytest.raises(native.PrayError):
+        native.Batch([sc], [native.pt_params(st, spp=2, max_depth=1, mode=native.PT_DIFFUSE)], [(rgb, None)])

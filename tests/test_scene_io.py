@@ -9,6 +9,7 @@ import tempfile
 import numpy as np
 import pytest
 
+from golden_util import load_scene_dump
 from nostrum_pray_gb300 import scenes
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -24,22 +25,7 @@ def _built():
 
 
 def load(json_path):
-    with tempfile.TemporaryDirectory() as td:
-        out = os.path.join(td, "scene.bin")
-        p = subprocess.run([DUMP, json_path, out], capture_output=True, text=True)
-        assert p.returncode == 0, p.stderr
-        raw = open(out, "rb").read()
-    info = np.frombuffer(raw[:17 * 8], np.float64)
-    n, nl = int(info[16]), int(info[15])
-    o = 17 * 8
-    verts = np.frombuffer(raw[o:o + 36 * n], np.float32).reshape(n, 9)
-    o += 36 * n
-    cols = np.frombuffer(raw[o:o + 12 * n], np.float32).reshape(n, 3)
-    o += 12 * n
-    emit = np.frombuffer(raw[o:o + n], np.uint8)
-    o += n
-    lights = np.frombuffer(raw[o:o + 24 * nl], np.float32).reshape(nl, 6)
-    return info, verts, cols, emit, lights
+    return load_scene_dump(json_path)
 
 
 def same(got, small, prefix):
