@@ -32,6 +32,10 @@ const int kConvs[][3] = {
 };
 constexpr int kNumConvs = 19;
 const int kEnc[5] = {32, 48, 64, 96, 128};
+// resolution level (size >> level) of each convolution
+const int kLevel[kNumConvs] = {0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 3, 3, 2, 2, 1, 1, 0, 0, 0};
+
+int pad16(int c) { return (c + 15) / 16 * 16; }
 
 template <class T>
 cudaError_t dalloc(T *&p, size_t n) {
@@ -69,11 +73,20 @@ cudaError_t Denoiser::init(uint64_t seed) {
         total += (size_t)c.cout * 9 * c.cin + c.cout;
     }
     n_params_ = total;
+    size_t tc_total = 0;
+    tc_off_.resize(kNumConvs);
+    for (int i = 0; i < kNumConvs; i++) {
+        tc_off_[i] = tc_total;
+        tc_total += dn::tc_packed_weight_elems(pad16(convs_[i].cin), convs_[i].cout);
+    }
+    plans_.assign(kNumConvs, dn::TcConvPlan{});
     cudaError_t e;
+    if ((e = cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) return e;
     if ((e = take(w_, total)) != cudaSuccess || (e = take(g_, total)) != cudaSuccess ||
         (e = take(m_, total)) != cudaSuccess || (e = take(v_, total)) != cudaSuccess ||
-        (e = take(wb_, total)) != cudaSuccess || (e = take(loss_, 1)) != cudaSuccess ||
-        (e = take(err_, 1)) != cudaSuccess || (e = cudaMemset(err_, 0, sizeof(int))) != cudaSuccess)
+        (e = take(wb_, total)) != cudaSuccess || (e = take(wtc_, tc_total)) != cudaSuccess ||
+        (e = take(loss_, 1)) != cudaSuccess || (e = take(err_, 1)) != cudaSuccess ||
+        (e = cudaMemset(err_, 0, sizeof(int))) != cudaSuccess)
         return e;
     // He-normal weights, zero biases, from the seed
     std::vector<float> h(total, 0.f);
@@ -92,13 +105,24 @@ cudaError_t Denoiser::init(uint64_t seed) {
         (e = cudaMemcpy(v_, zeros.data(), total * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
         return e;
     step_ = 0;
-    return dn::to_bf16(w_, wb_, total, 0);
+    if ((e = dn::to_bf16(w_, wb_, total, 0)) != cudaSuccess) return e;
+    return refresh_tc_weights(0);
+}
+
+cudaError_t Denoiser::refresh_tc_weights(cudaStream_t st) {
+    for (int i = 0; i < kNumConvs; i++) {
+        const Conv &c = convs_[i];
+        cudaError_t e = dn::tc_pack_weights(w_ + c.offset, wtc_ + tc_off_[i], c.cin, pad16(c.cin), c.cout, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t Denoiser::set_params(const float *host) {
     cudaError_t e = cudaMemcpy(w_, host, n_params_ * 4, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return e;
-    return dn::to_bf16(w_, wb_, n_params_, 0);
+    if ((e = dn::to_bf16(w_, wb_, n_params_, 0)) != cudaSuccess) return e;
+    return refresh_tc_weights(0);
 }
 
 cudaError_t Denoiser::get_params(float *host) const {
@@ -114,7 +138,10 @@ cudaError_t Denoiser::ensure(int n, int h, int w) {
     const size_t px = (size_t)n * h * w;
     if (px <= cap_pixels_ && h == h_ && w == w_dim_ && n == n_) return cudaSuccess;
     // keep the parameters, drop the activations
-    std::vector<void *> keep = {w_, g_, m_, v_, wb_, loss_, err_};
+    std::vector<void *> keep = {w_, g_, m_, v_, wb_, wtc_, loss_, err_};
+    partial_ = nullptr;
+    x16_ = nullptr;
+    plans_.assign(kNumConvs, dn::TcConvPlan{});
     for (void *p : owned_)
         if (std::find(keep.begin(), keep.end(), p) == keep.end()) cudaFree(p);
     owned_ = keep;
@@ -150,8 +177,18 @@ cudaError_t Denoiser::ensure(int n, int h, int w) {
         if ((e = act(l, kEnc[l], true)) != cudaSuccess) return e;
     }
     if ((e = take(out_, px * 3)) != cudaSuccess || (e = take(gout_, px * 3)) != cudaSuccess ||
-        (e = take(gtmp_, px * 128)) != cudaSuccess)
+        (e = take(gtmp_, px * 128)) != cudaSuccess || (e = take(x16_, px * pad16(kConvs[0][0]))) != cudaSuccess)
         return e;
+    // split-tap partial sums of the tensor-core kernel: the largest need of any convolution
+    size_t partial = 0;
+    for (int i = 0; i < kNumConvs; i++) {
+        dn::TcConvPlan shape;
+        const int l = kLevel[i];
+        if (dn::tc_conv_plan(shape, act_[0].x, n, h >> l, w >> l, pad16(kConvs[i][0]), kConvs[i][1], true,
+                             sm_count_) == cudaSuccess)
+            partial = std::max(partial, shape.partial_floats);
+    }
+    if (partial && (e = take(partial_, partial)) != cudaSuccess) return e;
     cap_pixels_ = px;
     return cudaSuccess;
 }
@@ -164,13 +201,29 @@ cudaError_t Denoiser::check(bool &ok) {
     return e;
 }
 
-cudaError_t Denoiser::conv_fwd(int ci, const Buf &in, Buf &out, cudaStream_t st) {
+cudaError_t Denoiser::conv_fwd(int ci, const Buf &in, __nv_bfloat16 *y, float *y32, cudaStream_t st) {
     const Conv &c = convs_[ci];
-    if (tensor_cores_)
-        return dn::conv3x3_forward_tc(in.x, wb_ + c.offset, w_ + c.offset + (size_t)c.cout * 9 * c.cin, out.x, nullptr,
-                                      n_, h_ >> in.level, w_dim_ >> in.level, c.cin, c.cout, c.relu, err_, st);
-    return dn::conv3x3_forward(in.x, wb_ + c.offset, w_ + c.offset + (size_t)c.cout * 9 * c.cin, out.x, nullptr, n_,
-                               h_ >> in.level, w_dim_ >> in.level, c.cin, c.cout, c.relu, st);
+    const int h = h_ >> in.level, w = w_dim_ >> in.level;
+    const float *bias = w_ + c.offset + (size_t)c.cout * 9 * c.cin;
+    if (!tensor_cores_)
+        return dn::conv3x3_forward(in.x, wb_ + c.offset, bias, y, y32, n_, h, w, c.cin, c.cout, c.relu, st);
+    const __nv_bfloat16 *x = in.x;
+    const int cin = pad16(c.cin);
+    if (cin != c.cin) {
+        if (in.level != 0) return cudaErrorInvalidValue;  // only the 10-channel input is padded
+        cudaError_t e = dn::pad_channels(in.x, x16_, (size_t)n_ * h * w, c.cin, cin, st);
+        if (e != cudaSuccess) return e;
+        x = x16_;
+    }
+    dn::TcConvPlan &pl = plans_[ci];
+    if (pl.x != x || pl.n != n_ || pl.h != h || pl.w != w) {
+        cudaError_t e = dn::tc_conv_plan(pl, x, n_, h, w, cin, c.cout, c.relu, sm_count_);
+        if (e != cudaSuccess) {
+            pl.x = nullptr;
+            return e;
+        }
+    }
+    return dn::conv3x3_forward_tc(pl, wtc_ + tc_off_[ci], bias, y, y32, partial_, err_, st);
 }
 
 cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h, int w, cudaStream_t st) {
@@ -189,9 +242,9 @@ cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h
             chk(dn::avgpool(src.x, act_[idx].x, n, h >> (l - 1), w >> (l - 1), src.c, st));
             prev = idx++;
         }
-        chk(conv_fwd(conv++, act_[prev], act_[idx], st));
+        chk(conv_fwd(conv++, act_[prev], act_[idx].x, nullptr, st));
         prev = idx++;
-        chk(conv_fwd(conv++, act_[prev], act_[idx], st));
+        chk(conv_fwd(conv++, act_[prev], act_[idx].x, nullptr, st));
         prev = idx++;
     }
     // decoder: prev = e4 (index 14)
@@ -205,19 +258,13 @@ cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h
         chk(dn::upsample(low.x, cat.x, n, h >> (l + 1), w >> (l + 1), low.c, cat.c, st));
         chk(dn::concat(skip.x, cat.x, p, skip.c, cat.c, low.c, st));
         prev = idx++;
-        chk(conv_fwd(conv++, act_[prev], act_[idx], st));
+        chk(conv_fwd(conv++, act_[prev], act_[idx].x, nullptr, st));
         prev = idx++;
-        chk(conv_fwd(conv++, act_[prev], act_[idx], st));
+        chk(conv_fwd(conv++, act_[prev], act_[idx].x, nullptr, st));
         prev = idx++;
     }
     // output convolution (no ReLU), FP32
-    const Conv &c = convs_[conv];
-    if (tensor_cores_)
-        chk(dn::conv3x3_forward_tc(act_[prev].x, wb_ + c.offset, w_ + c.offset + (size_t)c.cout * 9 * c.cin, nullptr,
-                                   out_, n, h, w, c.cin, c.cout, false, err_, st));
-    else
-        chk(dn::conv3x3_forward(act_[prev].x, wb_ + c.offset, w_ + c.offset + (size_t)c.cout * 9 * c.cin, nullptr,
-                                out_, n, h, w, c.cin, c.cout, false, st));
+    chk(conv_fwd(conv, act_[prev], nullptr, out_, st));
     // the network predicts a correction to the noisy input's log radiance
     chk(dn::add_input(out_, act_[0].x, px, st));
     return e;
@@ -289,7 +336,8 @@ cudaError_t Denoiser::backward(const float *target, cudaStream_t st) {
 
 cudaError_t Denoiser::apply_adam(float lr, cudaStream_t st) {
     step_++;
-    return dn::adam(w_, g_, m_, v_, wb_, n_params_, lr, 0.9f, 0.999f, 1e-8f, step_, st);
+    cudaError_t e = dn::adam(w_, g_, m_, v_, wb_, n_params_, lr, 0.9f, 0.999f, 1e-8f, step_, st);
+    return e == cudaSuccess ? refresh_tc_weights(st) : e;
 }
 
 cudaError_t Denoiser::output_radiance(float *out, cudaStream_t st) {

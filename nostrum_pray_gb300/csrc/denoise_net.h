@@ -51,7 +51,9 @@ class Denoiser {
     template <class T>
     cudaError_t take(T *&p, size_t n);
     cudaError_t ensure(int n, int h, int w);
-    cudaError_t conv_fwd(int ci, const Buf &in, Buf &out, cudaStream_t st);
+    cudaError_t conv_fwd(int ci, const Buf &in, __nv_bfloat16 *y, float *y32, cudaStream_t st);
+    // packed BF16 weights of the tensor-core kernel, from the FP32 master copy
+    cudaError_t refresh_tc_weights(cudaStream_t st);
     void release();
 
     std::vector<Conv> convs_;
@@ -62,6 +64,13 @@ class Denoiser {
     int n_ = 0, h_ = 0, w_dim_ = 0, step_ = 0;
     float *w_ = nullptr, *g_ = nullptr, *m_ = nullptr, *v_ = nullptr, *loss_ = nullptr;
     __nv_bfloat16 *wb_ = nullptr;
+    // tensor-core forward: packed weights (offsets per conv), the input padded
+    // to 16 channels, split-tap partial sums, one plan per convolution
+    __nv_bfloat16 *wtc_ = nullptr, *x16_ = nullptr;
+    std::vector<size_t> tc_off_;
+    float *partial_ = nullptr;
+    std::vector<dn::TcConvPlan> plans_;
+    int sm_count_ = 0;
     float *out_ = nullptr, *gout_ = nullptr, *gtmp_ = nullptr;
     int *err_ = nullptr;
     bool tensor_cores_ = true;

@@ -14,11 +14,28 @@
 namespace pray_gpu {
 namespace dn {
 
-// tcgen05 tensor-core version (denoise_tc.cu); *err is set to 1 if one of
-// its bounded mbarrier waits ran out
-cudaError_t conv3x3_forward_tc(const __nv_bfloat16 *x, const __nv_bfloat16 *w, const float *b, __nv_bfloat16 *y,
-                               float *y32, int n, int h, int wd, int cin, int cout, bool relu, int *err,
-                               cudaStream_t st);
+// tcgen05 tensor-core version (denoise_tc.cu). A plan holds the input's TMA
+// tensor map (the input buffer is fixed) and the launch shape; Cin must be a
+// multiple of 16 (pad_channels), the weights packed by tc_pack_weights
+// (cin_pad = Cin of the plan). Levels with few tiles split the taps over CTAs
+// and need `partial` (partial_floats floats). *err is set to 1 if one of the
+// kernel's bounded mbarrier waits ran out.
+struct TcConvPlan {
+    alignas(64) unsigned char tmap[128];  // CUtensorMap of x: (C, W, H, N), box (8, 10, 18, 1)
+    const __nv_bfloat16 *x;
+    int n, h, w, cin, cout, npad, relu;
+    int tiles_x, tiles_y, tiles, splits, taps_per_split, taps_per_stage, stages, tmem_cols;
+    uint32_t w_off, bar_off;
+    size_t smem, partial_floats;
+};
+cudaError_t tc_conv_plan(TcConvPlan &p, const __nv_bfloat16 *x, int n, int h, int w, int cin, int cout, bool relu,
+                         int sm_count);
+size_t tc_packed_weight_elems(int cin_pad, int cout);
+cudaError_t tc_pack_weights(const float *w, __nv_bfloat16 *packed, int cin, int cin_pad, int cout, cudaStream_t st);
+cudaError_t conv3x3_forward_tc(const TcConvPlan &p, const __nv_bfloat16 *wpacked, const float *bias,
+                               __nv_bfloat16 *y, float *y32, float *partial, int *err, cudaStream_t st);
+// y (pixels x cy) = x (pixels x c) followed by zero channels
+cudaError_t pad_channels(const __nv_bfloat16 *x, __nv_bfloat16 *y, size_t pixels, int c, int cy, cudaStream_t st);
 cudaError_t conv3x3_forward(const __nv_bfloat16 *x, const __nv_bfloat16 *w, const float *b, __nv_bfloat16 *y,
                             float *y32, int n, int h, int wd, int cin, int cout, bool relu, cudaStream_t st);
 // gpre: output gradient after the ReLU mask (FP32, n*h*w*cout); dx may be NULL

@@ -1,24 +1,34 @@
-// 3x3 convolution forward on the 5th-generation tensor cores (tcgen05).
+// 3x3 convolution forward on the 5th-generation tensor cores (tcgen05), BF16
+// operands, FP32 accumulation in tensor memory (TMEM).
 //
-// Implicit GEMM: D[pixel][cout] = sum_k A[pixel][k] B[cout][k], k = tap * Cin
-// + ci, A gathered from the NHWC activations with zero padding (im2col, never
-// materialised), B the [Cout][3][3][Cin] weights; BF16 operands, FP32
-// accumulation in tensor memory (TMEM).
+// Implicit GEMM without an im2col copy. One CTA (4 warps) computes a tile of
+// 16 x 8 output pixels (M = 128) x all output channels (N = Cout rounded up
+// to 16). The input halo of the tile, 18 x 10 pixels x Cin, is loaded once
+// by TMA (one 4-D tiled copy per 8-channel chunk; out-of-image pixels arrive
+// as zeros, which is the convolution's padding) into planes of
+// [y][x][8 channels] (16 bytes per pixel). In that layout the A operand of
+// tap (dy, dx) for 16 channels is the halo itself seen through a shared-memory
+// matrix descriptor: the tile's 8-pixel rows are the 8-row core-matrix
+// groups (stride 160 bytes = one halo row), the two 8-channel chunks are the
+// K-direction core matrices (stride = one plane), and the start address moves
+// by (dy * 10 + dx) * 16 bytes. So all nine taps read the same halo and the
+// threads gather nothing. The weights are packed once (tc_pack_weights) as
+// [tap][8-channel chunk][row][8] BF16 — exactly the no-swizzle K-major
+// core-matrix layout — and copied with plain bulk copies, all taps at once
+// when they fit or through a ring of per-tap stages. One thread issues the
+// kind::f16 MMAs (M 128, N Npad, K 16) and commits them to mbarriers.
 //
-// One CTA (4 warps) computes a 128-pixel x Npad tile (Npad = Cout rounded up
-// to 16, one TMEM column per output channel). Each stage gathers a 64-deep K
-// slice of A and B into shared memory in the no-swizzle K-major canonical
-// layout (8-row x 16-byte core matrices; neighbours along K 128 B apart,
-// along rows 256 B apart), fences it for the async proxy, and one thread
-// issues four kind::f16 MMAs (M 128, N Npad, K 16 each) and commits them to
-// an mbarrier. Two shared-memory stages alternate, so the gather of stage s+1
-// overlaps the MMAs of stage s. The epilogue reads the accumulator back with
-// tcgen05.ld (each warp its 32 TMEM lanes), adds the bias, applies ReLU and
-// stores BF16 (or FP32). Every mbarrier wait is bounded: on timeout the
-// kernel records an error, stops issuing, drains what it issued (again
-// bounded) and frees its TMEM.
+// The deep, small levels have too few tiles for 152 SMs: there the nine taps
+// are split over 3 or 9 CTAs per tile, each writing FP32 partial sums that a
+// second kernel adds in split order (deterministic) with the bias and ReLU.
+//
+// Every mbarrier wait is bounded: on timeout the kernel records an error,
+// stops issuing, waits (bounded) for the copies and MMAs it issued, and frees
+// its TMEM.
 #include <cstdint>
+#include <cstring>
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -27,28 +37,38 @@
 namespace pray_gpu {
 namespace dn {
 
+static_assert(sizeof(CUtensorMap) == sizeof(TcConvPlan::tmap), "tensor map size");
+
 namespace {
 
-constexpr int kTM = 128;         // pixels per tile (MMA M)
-constexpr int kKStage = 64;      // K per stage (4 MMAs of K 16)
-constexpr int kSubBytesA = kTM * 16 * 2;  // one 128 x 16 BF16 sub-tile
+constexpr int kTileW = 8, kTileH = 16;
+constexpr int kHaloW = kTileW + 2, kHaloH = kTileH + 2;
+constexpr uint32_t kChunkBytes = kHaloW * kHaloH * 16;  // one 8-channel halo plane (2880)
+constexpr uint32_t kPlaneBytes = 2944;                  // plane stride, 128-byte aligned
+constexpr uint32_t kRowBytes = kHaloW * 16;             // one halo row of one plane (160)
 constexpr uint32_t kWaitLimit = 1u << 24;
+constexpr size_t kSmemBudget = 110 * 1024;              // target per CTA (two or more CTAs per SM)
+constexpr size_t kSmemMax = 227 * 1024;
+constexpr size_t kSmemPerSm = 228 * 1024;
 
 struct TcArgs {
-    const __nv_bfloat16 *x;
-    const __nv_bfloat16 *w;
+    const __nv_bfloat16 *w;  // packed weights [tap][chunk][npad][8]
     const float *bias;
     __nv_bfloat16 *y;
     float *y32;
-    int n, h, wd, cin, cout, relu;
-    int K, Kpad, Npad, tmem_cols;
-    int *err;  // set to 1 if an mbarrier wait timed out
+    float *partial;          // [split][M][npad] when splits > 1
+    int n, h, wd, cin, cout, npad, relu;
+    int tiles_x, tiles_y;
+    int taps_per_split, taps_per_stage, stages;
+    int tmem_cols;
+    uint32_t w_off, bar_off;  // shared-memory offsets (the halo is at 0)
+    int *err;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// Shared-memory matrix descriptor: start, leading (K) and stride (row-group)
-// byte offsets, descriptor version 1, no swizzle.
+// Shared-memory matrix descriptor: start, leading (K-direction) and stride
+// (8-row group) byte offsets, descriptor version 1, no swizzle.
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
     return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
            (1ull << 46);
@@ -60,75 +80,81 @@ __host__ __device__ constexpr uint32_t inst_desc(int m, int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+__device__ __forceinline__ void mbar_init(uint32_t bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     for (uint32_t i = 0; i < kWaitLimit; i++) {
         uint32_t ok;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
             : "=r"(ok)
-            : "r"(addr), "r"(parity)
+            : "r"(bar), "r"(parity)
             : "memory");
         if (ok) return true;
     }
     return false;
 }
 
-// Byte offset of element (row, k) of a stage tile in the core-matrix layout:
-// sub-tile k / 16 (rows x 16), core matrix (row / 8, (k % 16) / 8), row % 8
-// at 16 B, k % 8 at 2 B.
-__device__ __forceinline__ uint32_t tile_off(int row, int k, int sub_bytes) {
-    return (uint32_t)((k >> 4) * sub_bytes + (row >> 3) * 256 + ((k >> 3) & 1) * 128 + (row & 7) * 16 + (k & 7) * 2);
+// One 8-channel chunk of the halo: box (8 channels, 10 x, 18 y, 1 image) at
+// (c, x, y, img); x and y may be -1 (zero fill).
+__device__ __forceinline__ void tma_halo(uint32_t dst, const CUtensorMap *map, uint32_t bar, int c, int x, int y,
+                                         int img) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, "
+        "%6}], [%2];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c), "r"(x), "r"(y), "r"(img)
+        : "memory");
 }
 
-__device__ __forceinline__ float bfv(__nv_bfloat16 v) { return __bfloat162float(v); }
-
-// Gathers 8 consecutive k (one 16-byte core-matrix row) of A for `pix`.
-__device__ __forceinline__ uint4 gather_a8(const TcArgs &P, int pix, int k0) {
-    alignas(16) __nv_bfloat16 v[8];
-    const int M = P.n * P.h * P.wd;
-    if (pix < M && (P.cin & 7) == 0 && k0 < P.K) {
-        const int tap = k0 / P.cin, ci = k0 - tap * P.cin;
-        const int xw = pix % P.wd, yh = (pix / P.wd) % P.h, img = pix / (P.wd * P.h);
-        const int sx = xw + tap % 3 - 1, sy = yh + tap / 3 - 1;
-        if (sx < 0 || sy < 0 || sx >= P.wd || sy >= P.h) return make_uint4(0, 0, 0, 0);
-        return *reinterpret_cast<const uint4 *>(P.x + (((size_t)img * P.h + sy) * P.wd + sx) * P.cin + ci);
-    }
-    for (int e = 0; e < 8; e++) {
-        const int k = k0 + e;
-        float val = 0.f;
-        if (pix < M && k < P.K) {
-            const int tap = k / P.cin, ci = k - tap * P.cin;
-            const int xw = pix % P.wd, yh = (pix / P.wd) % P.h, img = pix / (P.wd * P.h);
-            const int sx = xw + tap % 3 - 1, sy = yh + tap / 3 - 1;
-            if (sx >= 0 && sy >= 0 && sx < P.wd && sy < P.h)
-                val = bfv(P.x[(((size_t)img * P.h + sy) * P.wd + sx) * P.cin + ci]);
-        }
-        v[e] = __float2bfloat16(val);
-    }
-    return *reinterpret_cast<const uint4 *>(v);
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
 }
 
-// 8 consecutive k of B (weights) for output channel co.
-__device__ __forceinline__ uint4 gather_b8(const TcArgs &P, int co, int k0) {
-    alignas(16) __nv_bfloat16 v[8];
-    if (co < P.cout && (P.K & 7) == 0 && k0 < P.K)
-        return *reinterpret_cast<const uint4 *>(P.w + (size_t)co * P.K + k0);
-    for (int e = 0; e < 8; e++) {
-        const int k = k0 + e;
-        v[e] = (co < P.cout && k < P.K) ? P.w[(size_t)co * P.K + k] : __float2bfloat16(0.f);
-    }
-    return *reinterpret_cast<const uint4 *>(v);
+__device__ __forceinline__ void mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+        : "memory");
 }
 
-__global__ void __launch_bounds__(128) k_conv_tc(TcArgs P) {
-    extern __shared__ __align__(128) uint8_t smem[];
-    const int sub_b = P.Npad * 32;                       // one Npad x 16 BF16 sub-tile of B
-    const int stage_bytes = 4 * kSubBytesA + 4 * sub_b;  // A then B
-    uint8_t *stage0 = smem;
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + 2 * stage_bytes);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 2);
+__device__ __forceinline__ void commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+__global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtensorMap xmap, TcArgs P) {
+    extern __shared__ __align__(1024) uint8_t smem[];
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int m0 = blockIdx.x * kTM;
+    const int nchunk = P.cin >> 3;
+    const uint32_t halo = smem_u32(smem), wbase = halo + P.w_off;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + P.bar_off);
+    // bars[0] halo loaded, bars[1] all MMAs done, bars[2 + s] stage s loaded,
+    // bars[2 + stages + s] stage s consumed by its MMAs
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 + 2 * P.stages);
+    int *okflag = reinterpret_cast<int *>(tmem_slot + 1);
+    auto bar = [&](int i) { return smem_u32(&bars[i]); };
+
+    const int per_img = P.tiles_x * P.tiles_y;
+    const int img = blockIdx.x / per_img, rem = blockIdx.x - img * per_img;
+    const int y0 = (rem / P.tiles_x) * kTileH, x0 = (rem % P.tiles_x) * kTileW;
+    const int split = blockIdx.y;
+    const int t0 = split * P.taps_per_split;
+    const int nloads = P.taps_per_split / P.taps_per_stage;
+    const uint32_t wtap_bytes = (uint32_t)P.cin * P.npad * 2;
+    const uint32_t stage_bytes = wtap_bytes * P.taps_per_stage;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -137,78 +163,87 @@ __global__ void __launch_bounds__(128) k_conv_tc(TcArgs P) {
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[0])) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[1])) : "memory");
+        for (int i = 0; i < 2 + 2 * P.stages; i++) mbar_init(bar(i));
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-    const uint32_t idesc = inst_desc(kTM, P.Npad);
-    const int stages = P.Kpad / kKStage + ((P.Kpad % kKStage) ? 1 : 0);
-    uint32_t phase[2] = {0, 0};
-    bool issued[2] = {false, false};
-    bool ok = true;
 
-    for (int s = 0; s < stages && ok; s++) {
-        const int buf = s & 1;
-        uint8_t *A = stage0 + buf * stage_bytes;
-        uint8_t *B = A + 4 * kSubBytesA;
-        // the MMAs that last read this buffer must be done
-        if (issued[buf]) {
-            ok = mbar_wait(smem_u32(&mbar[buf]), phase[buf]);
-            phase[buf] ^= 1;
-            issued[buf] = false;
-            if (!ok) break;
+    if (tid == 0) {
+        bool ok = true;
+        // halo: one copy per 8-channel chunk, all completing on bars[0]
+        mbar_expect_tx(bar(0), (uint32_t)nchunk * kChunkBytes);
+        for (int c = 0; c < nchunk; c++) tma_halo(halo + c * kPlaneBytes, &xmap, bar(0), 8 * c, x0 - 1, y0 - 1, img);
+        // weights: the first `stages` loads
+        int issued = 0;
+        const __nv_bfloat16 *wsrc = P.w + (size_t)t0 * P.cin * P.npad;
+        for (; issued < nloads && issued < P.stages; issued++) {
+            mbar_expect_tx(bar(2 + issued), stage_bytes);
+            bulk_copy(wbase + issued * stage_bytes, wsrc + (size_t)issued * P.taps_per_stage * P.cin * P.npad,
+                      stage_bytes, bar(2 + issued));
         }
-        const int k0 = s * kKStage;
-        // A: 128 rows x 8 chunks of 8 k; B: Npad rows x 8 chunks
-        for (int i = tid; i < kTM * 8; i += 128) {
-            const int row = i >> 3, c = i & 7;
-            *reinterpret_cast<uint4 *>(A + tile_off(row, c * 8, kSubBytesA)) = gather_a8(P, m0 + row, k0 + c * 8);
-        }
-        for (int i = tid; i < P.Npad * 8; i += 128) {
-            const int row = i >> 3, c = i & 7;
-            *reinterpret_cast<uint4 *>(B + tile_off(row, c * 8, sub_b)) = gather_b8(P, row, k0 + c * 8);
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            for (int sub = 0; sub < 4; sub++) {
-                const int kk = k0 + sub * 16;
-                if (kk >= P.Kpad) break;
-                const uint64_t ad = smem_desc(smem_u32(A + sub * kSubBytesA), 128, 256);
-                const uint64_t bd = smem_desc(smem_u32(B + sub * sub_b), 128, 256);
-                const uint32_t acc = kk > 0 ? 1u : 0u;
-                asm volatile(
-                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-                    : "memory");
+        const bool halo_done = mbar_wait(bar(0), 0);
+        ok = halo_done;
+        const uint32_t idesc = inst_desc(128, P.npad);
+        int consumed = 0;
+        for (int j = 0; j < nloads && ok; j++) {
+            const int s = j % P.stages;
+            if (!mbar_wait(bar(2 + s), (uint32_t)(j / P.stages) & 1)) {
+                ok = false;
+                break;
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             smem_u32(&mbar[buf]))
-                         : "memory");
+            consumed = j + 1;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            for (int q = 0; q < P.taps_per_stage; q++) {
+                const int tap = t0 + j * P.taps_per_stage + q;
+                const int dy = tap / 3, dx = tap - 3 * (tap / 3);
+                const uint32_t a0 = halo + (uint32_t)(dy * kHaloW + dx) * 16;
+                const uint32_t b0 = wbase + s * stage_bytes + q * wtap_bytes;
+                for (int p = 0; p < nchunk / 2; p++) {
+                    const uint64_t ad = smem_desc(a0 + 2 * p * kPlaneBytes, kPlaneBytes, kRowBytes);
+                    const uint64_t bd = smem_desc(b0 + 2 * p * P.npad * 16, P.npad * 16, 128);
+                    mma(tmem, ad, bd, idesc, (j | q | p) != 0 ? 1u : 0u);
+                }
+            }
+            commit(bar(2 + P.stages + s));
+            // refill the stage of the previous load once its MMAs are done
+            // (this load's MMAs are queued behind them)
+            if (j >= 1 && issued < nloads) {
+                const int jp = j - 1, sp = jp % P.stages;
+                if (!mbar_wait(bar(2 + P.stages + sp), (uint32_t)(jp / P.stages) & 1)) {
+                    ok = false;
+                    break;
+                }
+                mbar_expect_tx(bar(2 + sp), stage_bytes);
+                bulk_copy(wbase + sp * stage_bytes, wsrc + (size_t)issued * P.taps_per_stage * P.cin * P.npad,
+                          stage_bytes, bar(2 + sp));
+                issued++;
+            }
         }
-        issued[buf] = true;
+        // all MMAs issued so far complete on bars[1]
+        commit(bar(1));
+        if (!ok) {
+            // drain copies still in flight (bounded) before the shared memory goes away
+            if (!halo_done) mbar_wait(bar(0), 0);
+            for (int j = consumed; j < issued; j++) mbar_wait(bar(2 + j % P.stages), (uint32_t)(j / P.stages) & 1);
+        }
+        *okflag = ok ? 1 : 0;
     }
-    // drain: wait for every committed group (bounded)
-    for (int b = 0; b < 2; b++)
-        if (issued[b]) {
-            if (!mbar_wait(smem_u32(&mbar[b]), phase[b])) ok = false;
-            phase[b] ^= 1;
-        }
-    if (!ok && tid == 0) atomicExch(P.err, 1);
+    __syncthreads();
+    const bool ok = mbar_wait(bar(1), 0) && *okflag;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     __syncthreads();
+    if (!ok && tid == 0) atomicExch(P.err, 1);
     if (ok) {
-        // epilogue: warp w holds TMEM lanes 32w..32w+31 = tile rows
-        const int row = warp * 32 + (tid & 31);
-        const int pix = m0 + row;
-        const int M = P.n * P.h * P.wd;
-        for (int c0 = 0; c0 < P.Npad; c0 += 16) {
+        // warp w holds TMEM lanes 32w..32w+31 = tile rows m: pixel (m / 8, m % 8)
+        const int m = warp * 32 + (tid & 31);
+        const int yy = y0 + (m >> 3), xx = x0 + (m & 7);
+        const bool valid = yy < P.h && xx < P.wd;
+        const size_t M = (size_t)P.n * P.h * P.wd;
+        const size_t pix = ((size_t)img * P.h + yy) * P.wd + xx;
+        for (int c0 = 0; c0 < P.npad; c0 += 16) {
             uint32_t r[16];
             const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
             asm volatile(
@@ -220,14 +255,31 @@ __global__ void __launch_bounds__(128) k_conv_tc(TcArgs P) {
                 : "r"(taddr)
                 : "memory");
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (pix < M) {
-                for (int j = 0; j < 16; j++) {
-                    const int co = c0 + j;
-                    if (co >= P.cout) break;
-                    float v = __uint_as_float(r[j]) + P.bias[co];
+            if (!valid) continue;
+            if (P.partial) {
+                float4 *o = reinterpret_cast<float4 *>(P.partial + ((size_t)split * M + pix) * P.npad + c0);
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    o[k] = make_float4(__uint_as_float(r[4 * k]), __uint_as_float(r[4 * k + 1]),
+                                       __uint_as_float(r[4 * k + 2]), __uint_as_float(r[4 * k + 3]));
+            } else if (P.y && (P.cout & 15) == 0) {
+                float v[16];
+#pragma unroll
+                for (int k = 0; k < 16; k++) {
+                    v[k] = __uint_as_float(r[k]) + __ldg(P.bias + c0 + k);
+                    if (P.relu) v[k] = fmaxf(v[k], 0.f);
+                }
+                uint4 *o = reinterpret_cast<uint4 *>(P.y + pix * P.cout + c0);
+                o[0] = make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
+                o[1] = make_uint4(pack2(v[8], v[9]), pack2(v[10], v[11]), pack2(v[12], v[13]), pack2(v[14], v[15]));
+            } else {
+#pragma unroll
+                for (int k = 0; k < 16; k++) {
+                    if (c0 + k >= P.cout) break;
+                    float v = __uint_as_float(r[k]) + __ldg(P.bias + c0 + k);
                     if (P.relu) v = fmaxf(v, 0.f);
-                    if (P.y) P.y[(size_t)pix * P.cout + co] = __float2bfloat16(v);
-                    if (P.y32) P.y32[(size_t)pix * P.cout + co] = v;
+                    if (P.y) P.y[pix * P.cout + c0 + k] = __float2bfloat16(v);
+                    if (P.y32) P.y32[pix * P.cout + c0 + k] = v;
                 }
             }
         }
@@ -241,32 +293,166 @@ __global__ void __launch_bounds__(128) k_conv_tc(TcArgs P) {
     }
 }
 
+// Sum of the split partials in split order, plus bias, ReLU, store.
+__global__ void k_conv_finalize(const float *partial, const float *bias, __nv_bfloat16 *y, float *y32, size_t M,
+                                int npad, int cout, int splits, int relu) {
+    const size_t total = M * (size_t)cout;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t pix = i / cout;
+        const int co = (int)(i - pix * cout);
+        float s = partial[pix * npad + co];
+        for (int k = 1; k < splits; k++) s = s + partial[((size_t)k * M + pix) * npad + co];
+        float v = s + bias[co];
+        if (relu) v = fmaxf(v, 0.f);
+        if (y) y[i] = __float2bfloat16(v);
+        if (y32) y32[i] = v;
+    }
+}
+
+// out[tap][chunk][row][8] from w[cout][9][cin] (zero rows and channels pad).
+__global__ void k_pack_weights(const float *w, __nv_bfloat16 *out, int cin, int cin_pad, int cout, int npad) {
+    const int nchunk = cin_pad >> 3;
+    const size_t total = (size_t)9 * cin_pad * npad;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int e = (int)(i & 7);
+        const size_t rowi = i >> 3;
+        const int r = (int)(rowi % npad);
+        const size_t ct = rowi / npad;
+        const int chunk = (int)(ct % nchunk), tap = (int)(ct / nchunk);
+        const int ci = chunk * 8 + e;
+        const float v = (r < cout && ci < cin) ? w[((size_t)r * 9 + tap) * cin + ci] : 0.f;
+        out[i] = __float2bfloat16(v);
+    }
+}
+
+__global__ void k_pad_channels(const __nv_bfloat16 *x, __nv_bfloat16 *y, size_t pixels, int c, int cy) {
+    const size_t total = pixels * cy;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t p = i / cy;
+        const int k = (int)(i - p * cy);
+        y[i] = k < c ? x[p * c + k] : __float2bfloat16(0.f);
+    }
+}
+
+unsigned grid_for(size_t n) {
+    const size_t b = (n + 255) / 256;
+    return (unsigned)(b < 4096 ? (b ? b : 1) : 4096);
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn() {
+    static EncodeTiled fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(p);
+    }
+    return fn;
+}
+
 }  // namespace
 
-cudaError_t conv3x3_forward_tc(const __nv_bfloat16 *x, const __nv_bfloat16 *w, const float *b, __nv_bfloat16 *y,
-                               float *y32, int n, int h, int wd, int cin, int cout, bool relu, int *err,
-                               cudaStream_t st) {
-    TcArgs P;
-    P.x = x, P.w = w, P.bias = b, P.y = y, P.y32 = y32;
-    P.n = n, P.h = h, P.wd = wd, P.cin = cin, P.cout = cout, P.relu = relu ? 1 : 0;
-    P.K = 9 * cin;
-    P.Kpad = (P.K + 15) / 16 * 16;
-    P.Npad = (cout + 15) / 16 * 16;
-    if (P.Npad > 256) return cudaErrorInvalidValue;
+size_t tc_packed_weight_elems(int cin_pad, int cout) { return (size_t)9 * cin_pad * ((cout + 15) / 16 * 16); }
+
+cudaError_t tc_pack_weights(const float *w, __nv_bfloat16 *packed, int cin, int cin_pad, int cout, cudaStream_t st) {
+    const int npad = (cout + 15) / 16 * 16;
+    k_pack_weights<<<grid_for(tc_packed_weight_elems(cin_pad, cout)), 256, 0, st>>>(w, packed, cin, cin_pad, cout,
+                                                                                   npad);
+    return cudaGetLastError();
+}
+
+cudaError_t pad_channels(const __nv_bfloat16 *x, __nv_bfloat16 *y, size_t pixels, int c, int cy, cudaStream_t st) {
+    k_pad_channels<<<grid_for(pixels * cy), 256, 0, st>>>(x, y, pixels, c, cy);
+    return cudaGetLastError();
+}
+
+cudaError_t tc_conv_plan(TcConvPlan &p, const __nv_bfloat16 *x, int n, int h, int w, int cin, int cout, bool relu,
+                         int sm_count) {
+    std::memset(&p, 0, sizeof(p));
+    if (n <= 0 || h <= 0 || w <= 0 || cin <= 0 || (cin & 15) || cin > 2040 || cout <= 0) return cudaErrorInvalidValue;
+    p.x = x, p.n = n, p.h = h, p.w = w, p.cin = cin, p.cout = cout, p.relu = relu ? 1 : 0;
+    p.npad = (cout + 15) / 16 * 16;
+    if (p.npad > 256) return cudaErrorInvalidValue;
+    p.tiles_x = (w + kTileW - 1) / kTileW;
+    p.tiles_y = (h + kTileH - 1) / kTileH;
+    const long long tiles = (long long)n * p.tiles_x * p.tiles_y;
+    if (tiles > 0x7FFFFFFFLL) return cudaErrorInvalidValue;
+    p.tiles = (int)tiles;
+    // split the taps when there are too few tiles to fill the GPU twice
+    p.splits = 1;
+    if (tiles < 2LL * sm_count) p.splits = (tiles * 3 >= 2LL * sm_count) ? 3 : 9;
+    p.taps_per_split = 9 / p.splits;
+    const size_t halo = (size_t)(cin / 8) * kPlaneBytes;
+    const size_t wtap = (size_t)cin * p.npad * 2;
+    if (halo + p.taps_per_split * wtap <= kSmemBudget) {
+        p.taps_per_stage = p.taps_per_split;
+        p.stages = 1;
+    } else {
+        p.taps_per_stage = 1;
+        size_t fit = halo < kSmemBudget ? (kSmemBudget - halo) / wtap : 0;
+        if (fit < 2) fit = 2;
+        p.stages = (int)(fit < (size_t)p.taps_per_split ? fit : (size_t)p.taps_per_split);
+    }
+    p.w_off = (uint32_t)halo;
+    p.bar_off = (uint32_t)(halo + (size_t)p.stages * p.taps_per_stage * wtap);
+    p.bar_off = (p.bar_off + 15) & ~15u;
+    size_t smem = p.bar_off + 8 * (2 + 2 * (size_t)p.stages) + 16;
     int cols = 32;
-    while (cols < P.Npad) cols <<= 1;
-    P.tmem_cols = cols;
-    P.err = err;
-    const int M = n * h * wd;
-    if (M <= 0) return cudaSuccess;
-    const size_t smem = 2 * (size_t)(4 * kSubBytesA + 4 * P.Npad * 32) + 64;
+    while (cols < p.npad) cols <<= 1;
+    p.tmem_cols = cols;
+    // no more CTAs per SM than TMEM has columns for (tcgen05.alloc would wait)
+    const size_t max_ctas = 512 / cols;
+    if (kSmemPerSm / (smem + 1024) > max_ctas) smem = kSmemPerSm / max_ctas - 1024 + 16;
+    if (smem > kSmemMax) return cudaErrorInvalidValue;
+    p.smem = smem;
+    p.partial_floats = p.splits > 1 ? (size_t)p.splits * n * h * w * p.npad : 0;
+
+    EncodeTiled enc = encode_fn();
+    if (!enc) return cudaErrorNotSupported;
+    const cuuint64_t dims[4] = {(cuuint64_t)cin, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
+    const cuuint64_t strides[3] = {(cuuint64_t)cin * 2, (cuuint64_t)w * cin * 2, (cuuint64_t)h * w * cin * 2};
+    const cuuint32_t box[4] = {8, kHaloW, kHaloH, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUtensorMap *map = reinterpret_cast<CUtensorMap *>(p.tmap);
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16 *>(x), dims, strides,
+                           box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+cudaError_t conv3x3_forward_tc(const TcConvPlan &p, const __nv_bfloat16 *wpacked, const float *bias,
+                               __nv_bfloat16 *y, float *y32, float *partial, int *err, cudaStream_t st) {
+    if (p.splits > 1 && !partial) return cudaErrorInvalidValue;
     static bool attr_set = false;
     if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaError_t e = cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
-    k_conv_tc<<<(M + kTM - 1) / kTM, 128, smem, st>>>(P);
+    TcArgs a;
+    a.w = wpacked, a.bias = bias;
+    a.y = p.splits > 1 ? nullptr : y;
+    a.y32 = p.splits > 1 ? nullptr : y32;
+    a.partial = p.splits > 1 ? partial : nullptr;
+    a.n = p.n, a.h = p.h, a.wd = p.w, a.cin = p.cin, a.cout = p.cout, a.npad = p.npad, a.relu = p.relu;
+    a.tiles_x = p.tiles_x, a.tiles_y = p.tiles_y;
+    a.taps_per_split = p.taps_per_split, a.taps_per_stage = p.taps_per_stage, a.stages = p.stages;
+    a.tmem_cols = p.tmem_cols;
+    a.w_off = p.w_off, a.bar_off = p.bar_off;
+    a.err = err;
+    CUtensorMap map;
+    std::memcpy(&map, p.tmap, sizeof(map));
+    k_conv_tc<<<dim3((unsigned)p.tiles, (unsigned)p.splits), 128, p.smem, st>>>(map, a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || p.splits == 1) return e;
+    const size_t M = (size_t)p.n * p.h * p.w;
+    k_conv_finalize<<<grid_for(M * p.cout), 256, 0, st>>>(partial, bias, y, y32, M, p.npad, p.cout, p.splits, p.relu);
     return cudaGetLastError();
 }
 

@@ -88,10 +88,14 @@ def test_features_match_oracle_hits(oracle):
     np.testing.assert_array_equal(got, want.astype(np.float16))
 
 
-@pytest.mark.parametrize("shape", [(1, 16, 16), (2, 48, 32)])
+@pytest.mark.parametrize("shape", [(1, 16, 16), (2, 48, 32), (2, 80, 48), (1, 256, 256)])
 def test_tensor_core_forward_matches_cuda_cores(shape):
     """The tcgen05 implicit-GEMM convolutions give the CUDA-core result (same
-    BF16 operands, FP32 accumulation; only the summation order differs)."""
+    BF16 operands, FP32 accumulation; only the summation order differs).
+    Shapes cover partial tiles (80 x 48 and 16 x 16 down to 5 x 3 and 1 x 1
+    at the deepest level), two images, and all three tap splits (1 at 256^2,
+    3 at 128^2, 9 below). Compared: the network's correction (output minus
+    input in log space), which every convolution feeds."""
     n, h, w = shape
     den = native.Denoiser(seed=9)
     rad, feat, _ = random_batch(4, n, h, w)
@@ -103,7 +107,10 @@ def test_tensor_core_forward_matches_cuda_cores(shape):
         den.denoise(t(rad), t(feat), out)
         den.check()
         outs.append(out.cpu().numpy())
+    base = np.log1p(rad.astype(np.float64))
+    corr = [np.log1p(o.astype(np.float64)) - base for o in outs]
     assert rel(np.log1p(outs[1].astype(np.float64)), np.log1p(outs[0].astype(np.float64))) < 5e-3
+    assert rel(corr[1], corr[0]) < 2e-2
 
 
 def test_trained_denoiser_beats_its_input():
