@@ -126,6 +126,7 @@ struct pray_scene {
         v.n_refs = (uint32_t)tree.refs.size();
         v.n_tris = (uint32_t)n_tris;
         v.tol = tol;
+        v.depth = (uint32_t)device_depth;
         v.emit_tris = d_emit;
         v.emit_cdf = d_emit_cdf;
         v.n_emit = n_emit;

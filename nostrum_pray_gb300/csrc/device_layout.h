@@ -52,6 +52,7 @@ struct DevScene {
     const GShade *shade;
     uint32_t n_nodes, n_refs, n_tris;
     float tol;  // absolute distance tolerance for culling boxes behind the origin
+    uint32_t depth;  // deepest node level of the hierarchy (root 0): a traversal pushes at most this many nodes
     // emitting triangles (for next-event estimation): geometry as GTri (v0.w
     // = triangle id) and the inclusive prefix sums of their areas
     const GTri *emit_tris;
