@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--dn-res", type=int, default=512, help="denoise: evaluation image size")
     ap.add_argument("--dn-train-res", type=int, default=512, help="denoise: training image size")
     ap.add_argument("--dn-cuda-cores", action="store_true", help="denoise-infer: CUDA-core convolutions")
+    ap.add_argument("--dn-spp-in", type=int, default=4, help="denoise: samples per pixel of the noisy input")
     ap.add_argument("--dn-ref-spp", type=int, default=1024, help="denoise: reference samples per pixel")
     ap.add_argument("--scheduler", choices=["pixel", "wavefront"], default="wavefront",
                     help="room workload: path-tracing scheduler")
@@ -421,7 +422,8 @@ def run_denoise(args):
     from nostrum_pray_gb300 import denoise as D, native
     torch.cuda.set_device(0)
     cfg = D.DenoiseConfig(res=args.dn_res, train_res=args.dn_train_res, spp_ref=args.dn_ref_spp,
-                          train_rooms=args.dn_train, eval_rooms=args.dn_eval, steps=args.dn_steps)
+                          train_rooms=args.dn_train, eval_rooms=args.dn_eval, steps=args.dn_steps,
+                          spp_in=args.dn_spp_in)
     t0 = time.perf_counter()
     train_seeds = list(range(cfg.seed, cfg.seed + cfg.train_rooms))
     eval_seeds = list(range(cfg.seed + 100_000, cfg.seed + 100_000 + cfg.eval_rooms))
@@ -455,7 +457,7 @@ def run_denoise(args):
             "relmse_final_mean": float(np.mean([r["relmse_final"] for r in rows])),
             "rooms_meeting_target": ok_d, "fallbacks": sum(r["fallback"] for r in rows), "fallback_spp": fb_spp,
             "time_plain_mean_s": float(np.mean(tp)) if tp else None, "time_denoised_mean_s": float(np.mean(td)),
-            "render_4spp_mean_s": float(np.mean([r["render_s"] for r in rows])),
+            "render_input_mean_s": float(np.mean([r["render_s"] for r in rows])),
             "inference_mean_s": float(np.mean([r["inference_s"] for r in rows])),
             "spp_plain_to_target": [r["spp_plain_to_target"] for r in rows],
             "loss_first_last": [losses[0][1], losses[-1][1]], "data_s": round(data_s, 1),
@@ -470,7 +472,7 @@ def run_denoise_infer(args):
     from nostrum_pray_gb300 import denoise as D, native
     torch.cuda.set_device(0)
     res = args.dn_res
-    cfg = D.DenoiseConfig(res=res, spp_ref=1)
+    cfg = D.DenoiseConfig(res=res, spp_ref=1, spp_in=args.dn_spp_in)
     st = D._setup(cfg)
     sc = native.Scene.from_setup(D.scenes.random_room(cfg.seed, grid=cfg.room_grid), st)
     rad = torch.empty((1, res, res, 3), dtype=torch.float32, device="cuda")
@@ -508,7 +510,7 @@ def run_denoise_infer(args):
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
             "config": {"workload": f"U-Net denoiser inference (19 3x3 convs, {D.num_params()} parameters, random "
-                                   f"initialisation), one {res}x{res} frame: 4-spp room render + features",
+                                   f"initialisation), one {res}x{res} frame: {cfg.spp_in}-spp room render + features",
                        "tensor_cores": not args.dn_cuda_cores, "l2": "flushed between steps"},
             "e2e": {"value": round(args.steps / (e2e_ms / 1e3), 2), "unit": "frames/s",
                     "h2d_bytes_per_step": rad.numel() * 4 + feat.numel() * 2, "d2h_bytes_per_step": out.numel() * 4},

@@ -267,9 +267,12 @@ typedef struct pray_denoiser pray_denoiser;
 /* Five-level convolutional U-Net (channels 32-48-64-96-128, two 3x3
  * convolutions with ReLU per level, 2x2 average pooling, nearest 2x
  * upsampling, concatenated skips, 3x3 output convolution), BF16 weights and
- * activations, FP32 accumulation. Input per pixel: log(1 + noisy radiance),
- * the 7 features; output: radiance, as log(1 + noisy radiance) plus the
- * network's correction. Weights He-initialised from seed (the output
+ * activations, FP32 accumulation. Radiance is demodulated: divided per
+ * channel by the first-hit albedo feature (clamped at 0) + 0.05 before the
+ * network and multiplied by it after. Input per pixel: log(1 + demodulated
+ * noisy radiance), the 7 features; output: radiance, as log(1 + demodulated
+ * noisy radiance) plus the network's correction, re-modulated. Weights
+ * He-initialised from seed (the output
  * convolution scaled by 0.1, so an untrained network returns its input).
  * Parameter vector: per convolution in forward order, weights
  * [cout][3][3][cin] then biases [cout]. */
@@ -282,8 +285,9 @@ pray_status pray_denoiser_set_params(pray_denoiser *d, const float *host);
  * features_dev n*h*w*7 FP16, out_dev n*h*w*3 floats (device pointers). */
 pray_status pray_denoise(pray_denoiser *d, const float *radiance_dev, const uint16_t *features_dev, int32_t n,
                          int32_t h, int32_t w, float *out_dev, void *stream);
-/* One Adam step (lr; betas 0.9 / 0.999) on the L1 loss between log(1 + output)
- * and log(1 + target_dev). loss_host (may be NULL) receives the loss before
+/* One Adam step (lr; betas 0.9 / 0.999) on the L1 loss between the network
+ * output and log(1 + target_dev / demodulation). loss_host (may be NULL)
+ * receives the loss before
  * the step (synchronises). */
 pray_status pray_denoiser_train_step(pray_denoiser *d, const float *radiance_dev, const uint16_t *features_dev,
                                      const float *target_dev, int32_t n, int32_t h, int32_t w, float lr,

@@ -210,9 +210,7 @@ cudaError_t Denoiser::conv_fwd(int ci, const Buf &in, __nv_bfloat16 *y, float *y
     const __nv_bfloat16 *x = in.x;
     const int cin = pad16(c.cin);
     if (cin != c.cin) {
-        if (in.level != 0) return cudaErrorInvalidValue;  // only the 10-channel input is padded
-        cudaError_t e = dn::pad_channels(in.x, x16_, (size_t)n_ * h * w, c.cin, cin, st);
-        if (e != cudaSuccess) return e;
+        if (ci != 0) return cudaErrorInvalidValue;  // only the 10-channel input is padded (by pack_input)
         x = x16_;
     }
     dn::TcConvPlan &pl = plans_[ci];
@@ -232,7 +230,8 @@ cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h
     if (e != cudaSuccess) return e;
     const size_t px = (size_t)n * h * w;
     auto chk = [&](cudaError_t x) { if (x != cudaSuccess && e == cudaSuccess) e = x; };
-    chk(dn::pack_input(rad, feat, act_[0].x, px, st));
+    feat_ = feat;
+    chk(dn::pack_input(rad, feat, act_[0].x, tensor_cores_ ? x16_ : nullptr, px, st));
     int conv = 0;
     // encoder
     int idx = 1, prev = 0;
@@ -255,8 +254,7 @@ cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h
         const Buf &low = act_[prev];
         const Buf &skip = act_[skip_idx[k]];
         const size_t p = (size_t)n * (h >> l) * (w >> l);
-        chk(dn::upsample(low.x, cat.x, n, h >> (l + 1), w >> (l + 1), low.c, cat.c, st));
-        chk(dn::concat(skip.x, cat.x, p, skip.c, cat.c, low.c, st));
+        chk(dn::upsample_concat(low.x, skip.x, cat.x, n, h >> (l + 1), w >> (l + 1), low.c, skip.c, st));
         prev = idx++;
         chk(conv_fwd(conv++, act_[prev], act_[idx].x, nullptr, st));
         prev = idx++;
@@ -279,7 +277,7 @@ cudaError_t Denoiser::backward(const float *target, cudaStream_t st) {
     chk(cudaMemsetAsync(loss_, 0, 4, st));
     for (Buf &b : act_)
         if (b.g) chk(cudaMemsetAsync(b.g, 0, (size_t)n * (h >> b.level) * (w >> b.level) * b.c * 4, st));
-    chk(dn::l1_loss(out_, target, gout_, loss_, px * 3, st));
+    chk(dn::l1_loss(out_, target, feat_, gout_, loss_, px * 3, st));
     auto conv_bwd = [&](int ci, Buf &in, const float *gpre, int level) {
         const Conv &c = convs_[ci];
         chk(dn::conv3x3_backward(in.x, wb_ + c.offset, gpre, in.g, g_ + c.offset,
@@ -341,7 +339,7 @@ cudaError_t Denoiser::apply_adam(float lr, cudaStream_t st) {
 }
 
 cudaError_t Denoiser::output_radiance(float *out, cudaStream_t st) {
-    return dn::expm1_out(out_, out, (size_t)n_ * h_ * w_dim_ * 3, st);
+    return dn::expm1_out(out_, feat_, out, (size_t)n_ * h_ * w_dim_ * 3, st);
 }
 
 }  // namespace pray_gpu

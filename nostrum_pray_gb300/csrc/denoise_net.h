@@ -22,7 +22,8 @@ class Denoiser {
     cudaError_t get_params(float *host) const;
     cudaError_t get_grads(float *host) const;
     // radiance: n*h*w*3 floats, feat: n*h*w*7 halves (albedo, normal, depth);
-    // h and w multiples of 16. The network output stays on the device.
+    // h and w multiples of 16. The network output stays on the device; feat
+    // must stay valid through the backward / output_radiance that follow.
     cudaError_t forward(const float *rad, const __half *feat, int n, int h, int w, cudaStream_t st);
     // after forward: L1 loss against the target radiance, all gradients
     cudaError_t backward(const float *target, cudaStream_t st);
@@ -72,6 +73,7 @@ class Denoiser {
     std::vector<dn::TcConvPlan> plans_;
     int sm_count_ = 0;
     float *out_ = nullptr, *gout_ = nullptr, *gtmp_ = nullptr;
+    const __half *feat_ = nullptr;  // features of the last forward (the caller's buffer; used until the call returns)
     int *err_ = nullptr;
     bool tensor_cores_ = true;
 };

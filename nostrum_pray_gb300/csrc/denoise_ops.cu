@@ -225,21 +225,7 @@ __global__ void k_avgpool_bwd(const float *gy, float *gx, int n, int h, int w, i
 }
 
 // nearest 2x upsampling of x (c channels) into channels [0, c) of y (cy channels)
-__global__ void k_upsample(const __nv_bfloat16 *x, __nv_bfloat16 *y, int n, int h, int w, int c, int cy) {
-    const int H = 2 * h, W = 2 * w;
-    const size_t total = (size_t)n * H * W * c;
-    for (size_t i = gtid(); i < total; i += gstride()) {
-        const int ch = (int)(i % c);
-        size_t r = i / c;
-        const int xx = (int)(r % W);
-        r /= W;
-        const int yy = (int)(r % H);
-        const int img = (int)(r / H);
-        y[(((size_t)img * H + yy) * W + xx) * cy + ch] = x[(((size_t)img * h + yy / 2) * w + xx / 2) * c + ch];
-    }
-}
-
-// gradient of k_upsample: gx[h,w] = sum of the 4 children (channels [0,c) of gy)
+// gradient of the nearest 2x upsampling: gx[h,w] = sum of the 4 children (channels [0,c) of gy)
 __global__ void k_upsample_bwd(const float *gy, float *gx, int n, int h, int w, int c, int cy) {
     const int W = 2 * w;
     const size_t total = (size_t)n * h * w * c;
@@ -255,34 +241,45 @@ __global__ void k_upsample_bwd(const float *gy, float *gx, int n, int h, int w, 
     }
 }
 
-// copy x (c channels) into channels [off, off+c) of y (cy channels)
-__global__ void k_concat(const __nv_bfloat16 *x, __nv_bfloat16 *y, size_t pixels, int c, int cy, int off) {
-    const size_t total = pixels * c;
-    for (size_t i = gtid(); i < total; i += gstride()) y[(i / c) * cy + off + i % c] = x[i];
-}
-
 // gx (c channels) += channels [off, off+c) of gy (cy channels)
 __global__ void k_split_add(const float *gy, float *gx, size_t pixels, int c, int cy, int off) {
     const size_t total = pixels * c;
     for (size_t i = gtid(); i < total; i += gstride()) gx[i] += gy[(i / c) * cy + off + i % c];
 }
 
-// network input: log1p(radiance) 3, albedo 3, normal 3, depth 1 from FP16
-// feature buffers (radiance n x 3 floats, features n x 7 halves)
-__global__ void k_pack_input(const float *rad, const __half *feat, __nv_bfloat16 *x, size_t pixels) {
+// Demodulation divisor of value i (pixel i / 3): first-hit albedo of its
+// channel, clamped at 0, plus 0.05.
+__device__ __forceinline__ float demod(const __half *feat, size_t i) {
+    return fmaxf(__half2float(feat[7 * (i / 3) + i % 3]), 0.f) + kDemodFloor;
+}
+
+// network input: log1p(radiance / demodulation) 3, albedo 3, normal 3, depth
+// 1 from FP16 feature buffers (radiance n x 3 floats, features n x 7 halves);
+// x16 (optional) receives the same 10 channels padded to 16 with zeros
+__global__ void k_pack_input(const float *rad, const __half *feat, __nv_bfloat16 *x, __nv_bfloat16 *x16,
+                             size_t pixels) {
     for (size_t p = gtid(); p < pixels; p += gstride()) {
-        for (int k = 0; k < 3; k++) x[p * 10 + k] = __float2bfloat16(log1pf(fmaxf(rad[3 * p + k], 0.f)));
-        for (int k = 0; k < 7; k++) x[p * 10 + 3 + k] = __float2bfloat16(__half2float(feat[7 * p + k]));
+        __nv_bfloat16 v[16];
+        for (int k = 0; k < 3; k++) v[k] = __float2bfloat16(log1pf(fmaxf(rad[3 * p + k], 0.f) / demod(feat, 3 * p + k)));
+        for (int k = 0; k < 7; k++) v[3 + k] = __float2bfloat16(__half2float(feat[7 * p + k]));
+        for (int k = 10; k < 16; k++) v[k] = __float2bfloat16(0.f);
+        for (int k = 0; k < 10; k++) x[p * 10 + k] = v[k];
+        if (x16) {
+            uint4 *o = reinterpret_cast<uint4 *>(x16 + p * 16);
+            o[0] = *reinterpret_cast<const uint4 *>(v);
+            o[1] = *reinterpret_cast<const uint4 *>(v + 8);
+        }
     }
 }
 
-// L1 loss on log1p(radiance): out = network output (log space), target in
-// linear radiance; loss sum into loss[0], gradient into g (scaled by 1/n)
-__global__ void k_l1(const float *out, const float *target, float *g, float *loss, size_t n) {
+// L1 loss on log1p(radiance / demodulation): out = network output (log
+// space), target in linear radiance; loss sum into loss[0], gradient into g
+// (scaled by 1/n)
+__global__ void k_l1(const float *out, const float *target, const __half *feat, float *g, float *loss, size_t n) {
     float acc = 0.f;
     const float inv = 1.f / (float)n;
     for (size_t i = gtid(); i < n; i += gstride()) {
-        const float d = out[i] - log1pf(fmaxf(target[i], 0.f));
+        const float d = out[i] - log1pf(fmaxf(target[i], 0.f) / demod(feat, i));
         acc += fabsf(d);
         g[i] = (d > 0.f ? 1.f : (d < 0.f ? -1.f : 0.f)) * inv;
     }
@@ -295,8 +292,31 @@ __global__ void k_add_input(float *out, const __nv_bfloat16 *x0, size_t pixels) 
     for (size_t i = gtid(); i < pixels * 3; i += gstride()) out[i] += bf(x0[(i / 3) * 10 + i % 3]);
 }
 
-__global__ void k_expm1(const float *out, float *rad, size_t n) {
-    for (size_t i = gtid(); i < n; i += gstride()) rad[i] = expm1f(out[i]);
+__global__ void k_expm1(const float *out, const __half *feat, float *rad, size_t n) {
+    for (size_t i = gtid(); i < n; i += gstride()) rad[i] = expm1f(out[i]) * demod(feat, i);
+}
+
+// cat (c + cs channels, 2h x 2w) = [nearest 2x upsampling of low (c
+// channels, h x w), skip (cs channels, 2h x 2w)], 8 channels (16 bytes) per
+// thread; c and cs multiples of 8
+__global__ void k_upsample_concat(const __nv_bfloat16 *low, const __nv_bfloat16 *skip, __nv_bfloat16 *cat, int n,
+                                  int h, int w, int c, int cs) {
+    const int H = 2 * h, W = 2 * w, cy = c + cs, chunks = cy / 8;
+    const size_t total = (size_t)n * H * W * chunks;
+    for (size_t i = gtid(); i < total; i += gstride()) {
+        const int k = (int)(i % chunks);
+        const size_t pix = i / chunks;
+        const int xx = (int)(pix % W);
+        const size_t r = pix / W;
+        const int yy = (int)(r % H);
+        const int img = (int)(r / H);
+        uint4 v;
+        if (8 * k < c)
+            v = *reinterpret_cast<const uint4 *>(low + (((size_t)img * h + yy / 2) * w + xx / 2) * c + 8 * k);
+        else
+            v = *reinterpret_cast<const uint4 *>(skip + pix * cs + (8 * k - c));
+        *reinterpret_cast<uint4 *>(cat + pix * cy + 8 * k) = v;
+    }
 }
 
 __global__ void k_adam(float *w, const float *g, float *m, float *v, __nv_bfloat16 *wb, size_t n, float lr, float b1,
@@ -359,36 +379,37 @@ cudaError_t avgpool_backward(const float *gy, float *gx, int n, int h, int w, in
     k_avgpool_bwd<<<blocks_for((size_t)n * h * w * c), 256, 0, st>>>(gy, gx, n, h, w, c);
     return cudaGetLastError();
 }
-cudaError_t upsample(const __nv_bfloat16 *x, __nv_bfloat16 *y, int n, int h, int w, int c, int cy, cudaStream_t st) {
-    k_upsample<<<blocks_for((size_t)n * h * w * c * 4), 256, 0, st>>>(x, y, n, h, w, c, cy);
-    return cudaGetLastError();
-}
 cudaError_t upsample_backward(const float *gy, float *gx, int n, int h, int w, int c, int cy, cudaStream_t st) {
     k_upsample_bwd<<<blocks_for((size_t)n * h * w * c), 256, 0, st>>>(gy, gx, n, h, w, c, cy);
-    return cudaGetLastError();
-}
-cudaError_t concat(const __nv_bfloat16 *x, __nv_bfloat16 *y, size_t pixels, int c, int cy, int off, cudaStream_t st) {
-    k_concat<<<blocks_for(pixels * c), 256, 0, st>>>(x, y, pixels, c, cy, off);
     return cudaGetLastError();
 }
 cudaError_t split_add(const float *gy, float *gx, size_t pixels, int c, int cy, int off, cudaStream_t st) {
     k_split_add<<<blocks_for(pixels * c), 256, 0, st>>>(gy, gx, pixels, c, cy, off);
     return cudaGetLastError();
 }
-cudaError_t pack_input(const float *rad, const __half *feat, __nv_bfloat16 *x, size_t pixels, cudaStream_t st) {
-    k_pack_input<<<blocks_for(pixels), 256, 0, st>>>(rad, feat, x, pixels);
+cudaError_t upsample_concat(const __nv_bfloat16 *low, const __nv_bfloat16 *skip, __nv_bfloat16 *cat, int n, int h,
+                            int w, int c, int cs, cudaStream_t st) {
+    if ((c & 7) || (cs & 7)) return cudaErrorInvalidValue;
+    k_upsample_concat<<<blocks_for((size_t)n * 4 * h * w * ((c + cs) / 8)), 256, 0, st>>>(low, skip, cat, n, h, w, c,
+                                                                                         cs);
     return cudaGetLastError();
 }
-cudaError_t l1_loss(const float *out, const float *target, float *g, float *loss, size_t n, cudaStream_t st) {
-    k_l1<<<blocks_for(n), 256, 0, st>>>(out, target, g, loss, n);
+cudaError_t pack_input(const float *rad, const __half *feat, __nv_bfloat16 *x, __nv_bfloat16 *x16, size_t pixels,
+                       cudaStream_t st) {
+    k_pack_input<<<blocks_for(pixels), 256, 0, st>>>(rad, feat, x, x16, pixels);
+    return cudaGetLastError();
+}
+cudaError_t l1_loss(const float *out, const float *target, const __half *feat, float *g, float *loss, size_t n,
+                    cudaStream_t st) {
+    k_l1<<<blocks_for(n), 256, 0, st>>>(out, target, feat, g, loss, n);
     return cudaGetLastError();
 }
 cudaError_t add_input(float *out, const __nv_bfloat16 *x0, size_t pixels, cudaStream_t st) {
     k_add_input<<<blocks_for(pixels * 3), 256, 0, st>>>(out, x0, pixels);
     return cudaGetLastError();
 }
-cudaError_t expm1_out(const float *out, float *rad, size_t n, cudaStream_t st) {
-    k_expm1<<<blocks_for(n), 256, 0, st>>>(out, rad, n);
+cudaError_t expm1_out(const float *out, const __half *feat, float *rad, size_t n, cudaStream_t st) {
+    k_expm1<<<blocks_for(n), 256, 0, st>>>(out, feat, rad, n);
     return cudaGetLastError();
 }
 cudaError_t adam(float *w, const float *g, float *m, float *v, __nv_bfloat16 *wb, size_t n, float lr, float b1,

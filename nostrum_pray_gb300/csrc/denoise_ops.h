@@ -16,7 +16,7 @@ namespace dn {
 
 // tcgen05 tensor-core version (denoise_tc.cu). A plan holds the input's TMA
 // tensor map (the input buffer is fixed) and the launch shape; Cin must be a
-// multiple of 16 (pad_channels), the weights packed by tc_pack_weights
+// multiple of 16 (pack_input pads the network input), the weights packed by tc_pack_weights
 // (cin_pad = Cin of the plan). Levels with few tiles split the taps over CTAs
 // and need `partial` (partial_floats floats). *err is set to 1 if one of the
 // kernel's bounded mbarrier waits ran out.
@@ -34,8 +34,6 @@ size_t tc_packed_weight_elems(int cin_pad, int cout);
 cudaError_t tc_pack_weights(const float *w, __nv_bfloat16 *packed, int cin, int cin_pad, int cout, cudaStream_t st);
 cudaError_t conv3x3_forward_tc(const TcConvPlan &p, const __nv_bfloat16 *wpacked, const float *bias,
                                __nv_bfloat16 *y, float *y32, float *partial, int *err, cudaStream_t st);
-// y (pixels x cy) = x (pixels x c) followed by zero channels
-cudaError_t pad_channels(const __nv_bfloat16 *x, __nv_bfloat16 *y, size_t pixels, int c, int cy, cudaStream_t st);
 cudaError_t conv3x3_forward(const __nv_bfloat16 *x, const __nv_bfloat16 *w, const float *b, __nv_bfloat16 *y,
                             float *y32, int n, int h, int wd, int cin, int cout, bool relu, cudaStream_t st);
 // gpre: output gradient after the ReLU mask (FP32, n*h*w*cout); dx may be NULL
@@ -44,14 +42,22 @@ cudaError_t conv3x3_backward(const __nv_bfloat16 *x, const __nv_bfloat16 *w, con
 cudaError_t relu_mask(const __nv_bfloat16 *y, const float *g, float *out, size_t n, cudaStream_t st);
 cudaError_t avgpool(const __nv_bfloat16 *x, __nv_bfloat16 *y, int n, int h, int w, int c, cudaStream_t st);
 cudaError_t avgpool_backward(const float *gy, float *gx, int n, int h, int w, int c, cudaStream_t st);
-cudaError_t upsample(const __nv_bfloat16 *x, __nv_bfloat16 *y, int n, int h, int w, int c, int cy, cudaStream_t st);
 cudaError_t upsample_backward(const float *gy, float *gx, int n, int h, int w, int c, int cy, cudaStream_t st);
-cudaError_t concat(const __nv_bfloat16 *x, __nv_bfloat16 *y, size_t pixels, int c, int cy, int off, cudaStream_t st);
 cudaError_t split_add(const float *gy, float *gx, size_t pixels, int c, int cy, int off, cudaStream_t st);
-cudaError_t pack_input(const float *rad, const __half *feat, __nv_bfloat16 *x, size_t pixels, cudaStream_t st);
-cudaError_t l1_loss(const float *out, const float *target, float *g, float *loss, size_t n, cudaStream_t st);
+// Radiance is demodulated by the first-hit albedo: divided by
+// max(albedo, 0) + kDemodFloor (per channel) on the way in and in the loss's
+// target, multiplied back on the way out.
+constexpr float kDemodFloor = 0.05f;
+// x: 10 channels; x16 (may be NULL): the same padded to 16 channels
+cudaError_t pack_input(const float *rad, const __half *feat, __nv_bfloat16 *x, __nv_bfloat16 *x16, size_t pixels,
+                       cudaStream_t st);
+// cat = [nearest 2x upsampling of low (c channels, h x w), skip (cs channels)]
+cudaError_t upsample_concat(const __nv_bfloat16 *low, const __nv_bfloat16 *skip, __nv_bfloat16 *cat, int n, int h,
+                            int w, int c, int cs, cudaStream_t st);
+cudaError_t l1_loss(const float *out, const float *target, const __half *feat, float *g, float *loss, size_t n,
+                    cudaStream_t st);
 cudaError_t add_input(float *out, const __nv_bfloat16 *x0, size_t pixels, cudaStream_t st);
-cudaError_t expm1_out(const float *out, float *rad, size_t n, cudaStream_t st);
+cudaError_t expm1_out(const float *out, const __half *feat, float *rad, size_t n, cudaStream_t st);
 cudaError_t adam(float *w, const float *g, float *m, float *v, __nv_bfloat16 *wb, size_t n, float lr, float b1,
                  float b2, float eps, int step, cudaStream_t st);
 cudaError_t to_bf16(const float *a, __nv_bfloat16 *b, size_t n, cudaStream_t st);

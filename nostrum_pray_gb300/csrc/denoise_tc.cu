@@ -293,19 +293,31 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtenso
     }
 }
 
-// Sum of the split partials in split order, plus bias, ReLU, store.
+// Sum of the split partials in split order, plus bias, ReLU, store; four
+// channels per thread (cout a multiple of 4).
 __global__ void k_conv_finalize(const float *partial, const float *bias, __nv_bfloat16 *y, float *y32, size_t M,
                                 int npad, int cout, int splits, int relu) {
-    const size_t total = M * (size_t)cout;
+    const int groups = cout / 4;
+    const size_t total = M * (size_t)groups;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        const size_t pix = i / cout;
-        const int co = (int)(i - pix * cout);
-        float s = partial[pix * npad + co];
-        for (int k = 1; k < splits; k++) s = s + partial[((size_t)k * M + pix) * npad + co];
-        float v = s + bias[co];
-        if (relu) v = fmaxf(v, 0.f);
-        if (y) y[i] = __float2bfloat16(v);
-        if (y32) y32[i] = v;
+        const size_t pix = i / groups;
+        const int co = 4 * (int)(i - pix * groups);
+        float4 s = *reinterpret_cast<const float4 *>(partial + pix * npad + co);
+        for (int k = 1; k < splits; k++) {
+            const float4 q = *reinterpret_cast<const float4 *>(partial + ((size_t)k * M + pix) * npad + co);
+            s.x = s.x + q.x, s.y = s.y + q.y, s.z = s.z + q.z, s.w = s.w + q.w;
+        }
+        const float4 b = *reinterpret_cast<const float4 *>(bias + co);
+        float v[4] = {s.x + b.x, s.y + b.y, s.z + b.z, s.w + b.w};
+        if (relu)
+            for (int k = 0; k < 4; k++) v[k] = fmaxf(v[k], 0.f);
+        if (y) {
+            uint2 o;
+            o.x = pack2(v[0], v[1]);
+            o.y = pack2(v[2], v[3]);
+            *reinterpret_cast<uint2 *>(y + pix * cout + co) = o;
+        }
+        if (y32) *reinterpret_cast<float4 *>(y32 + pix * cout + co) = make_float4(v[0], v[1], v[2], v[3]);
     }
 }
 
@@ -322,15 +334,6 @@ __global__ void k_pack_weights(const float *w, __nv_bfloat16 *out, int cin, int 
         const int ci = chunk * 8 + e;
         const float v = (r < cout && ci < cin) ? w[((size_t)r * 9 + tap) * cin + ci] : 0.f;
         out[i] = __float2bfloat16(v);
-    }
-}
-
-__global__ void k_pad_channels(const __nv_bfloat16 *x, __nv_bfloat16 *y, size_t pixels, int c, int cy) {
-    const size_t total = pixels * cy;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        const size_t p = i / cy;
-        const int k = (int)(i - p * cy);
-        y[i] = k < c ? x[p * c + k] : __float2bfloat16(0.f);
     }
 }
 
@@ -364,11 +367,6 @@ cudaError_t tc_pack_weights(const float *w, __nv_bfloat16 *packed, int cin, int 
     const int npad = (cout + 15) / 16 * 16;
     k_pack_weights<<<grid_for(tc_packed_weight_elems(cin_pad, cout)), 256, 0, st>>>(w, packed, cin, cin_pad, cout,
                                                                                    npad);
-    return cudaGetLastError();
-}
-
-cudaError_t pad_channels(const __nv_bfloat16 *x, __nv_bfloat16 *y, size_t pixels, int c, int cy, cudaStream_t st) {
-    k_pad_channels<<<grid_for(pixels * cy), 256, 0, st>>>(x, y, pixels, c, cy);
     return cudaGetLastError();
 }
 
@@ -428,7 +426,7 @@ cudaError_t tc_conv_plan(TcConvPlan &p, const __nv_bfloat16 *x, int n, int h, in
 
 cudaError_t conv3x3_forward_tc(const TcConvPlan &p, const __nv_bfloat16 *wpacked, const float *bias,
                                __nv_bfloat16 *y, float *y32, float *partial, int *err, cudaStream_t st) {
-    if (p.splits > 1 && !partial) return cudaErrorInvalidValue;
+    if (p.splits > 1 && (!partial || (p.cout & 3))) return cudaErrorInvalidValue;
     static bool attr_set = false;
     if (!attr_set) {
         cudaError_t e = cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax);
@@ -452,7 +450,8 @@ cudaError_t conv3x3_forward_tc(const TcConvPlan &p, const __nv_bfloat16 *wpacked
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || p.splits == 1) return e;
     const size_t M = (size_t)p.n * p.h * p.w;
-    k_conv_finalize<<<grid_for(M * p.cout), 256, 0, st>>>(partial, bias, y, y32, M, p.npad, p.cout, p.splits, p.relu);
+    k_conv_finalize<<<grid_for(M * p.cout / 4), 256, 0, st>>>(partial, bias, y, y32, M, p.npad, p.cout, p.splits,
+                                                               p.relu);
     return cudaGetLastError();
 }
 

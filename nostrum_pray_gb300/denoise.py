@@ -4,8 +4,9 @@ evaluation of the U-Net (pray_denoiser_* in include/nostrum_pray.h).
 Data: seeded procedural rooms (scenes.random_room), each rendered with the
 next-event-estimation path tracer at a few samples per pixel (the noisy
 input), with its first-hit features, and at many samples per pixel
-accumulated in FP64 (the reference). Radiance is divided by the first-hit
-albedo (+0.05) before the network and multiplied back after it. The network
+accumulated in FP64 (the reference). The denoiser divides radiance by the
+first-hit albedo (+0.05) before the network and multiplies it back after
+(pray_denoise). The network
 is trained by its own CUDA forward/backward kernels with an L1 loss in
 log(1 + radiance) space and Adam, on random crops.
 
@@ -91,12 +92,6 @@ def render_room(cfg: DenoiseConfig, room_seed: int, torch, res: Optional[int] = 
     return sc, rad, feat, ref
 
 
-def demodulation(feat, torch):
-    """First-hit albedo (+0.05) per pixel: the network denoises radiance /
-    albedo (irradiance-like, smoother) and the result is multiplied back."""
-    return feat[..., 0:3].to(torch.float32).clamp_min(0.0) + 0.05
-
-
 def relmse(img, ref, torch) -> float:
     """FP64 relMSE on the device (pray_relmse)."""
     out = torch.zeros(1, dtype=torch.float64, device="cuda")
@@ -117,9 +112,7 @@ def make_dataset(cfg: DenoiseConfig, seeds: List[int], torch, res: Optional[int]
 
 def train(den: native.Denoiser, rad, feat, ref, cfg: DenoiseConfig, torch, log_every: int = 100):
     n = rad.shape[0]
-    dm = demodulation(feat, torch)
-    rad = (rad / dm).contiguous()
-    target = (ref.to(torch.float32) / dm).contiguous()
+    target = ref.to(torch.float32).contiguous()
     g = torch.Generator(device="cpu").manual_seed(cfg.seed)
     losses = []
     size = rad.shape[1]
@@ -178,27 +171,20 @@ def denoised_eval(cfg: DenoiseConfig, den, sc, ref, room_seed: int, torch):
     p2 = _params(cfg, st, cfg.spp_in, seed=room_seed * 7 + 6)
     pf = _params(cfg, st, 1, seed=0)
 
-    demod_in = torch.empty_like(rad)
-
     def run():
         sc.render_pt(p, None, rad[0])
         sc.render_features(pf, feat[0])
-        dm = demodulation(feat, torch)
-        torch.div(rad, dm, out=demod_in)
-        den.denoise(demod_in, feat, out)
-        out.mul_(dm)
+        den.denoise(rad, feat, out)
 
     run()
     t = timed(run, torch)
     t_render = timed(lambda: sc.render_pt(p, None, rad[0]), torch)
-    t_infer = timed(lambda: den.denoise(demod_in, feat, out), torch)
+    t_infer = timed(lambda: den.denoise(rad, feat, out), torch)
     run()
     e = relmse(out[0], ref, torch)
     e_noisy = relmse(rad[0], ref, torch)
     sc.render_pt(p2, None, rad2[0])
-    dm = demodulation(feat, torch)
-    den.denoise((rad2 / dm).contiguous(), feat, out2)
-    out2.mul_(dm)
+    den.denoise(rad2, feat, out2)
     pred = 0.5 * relmse(out[0], out2[0].to(torch.float64), torch)
     return {"relmse_denoised": e, "relmse_noisy": e_noisy, "time_s": t, "render_s": t_render,
             "inference_s": t_infer, "predicted": pred}

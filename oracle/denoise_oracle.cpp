@@ -143,6 +143,13 @@ T up_cat(const T &low, const T &skip) {
     return y;
 }
 
+// Demodulation divisor of radiance value i: first-hit albedo of its channel
+// (feature i % 3 of pixel i / 3), clamped at 0, plus 0.05, in float as on the
+// device.
+float demod(const uint16_t *feat, size_t i) {
+    return std::fmax((float)half_to_double(feat[7 * (i / 3) + i % 3]), 0.f) + 0.05f;
+}
+
 }  // namespace
 
 extern "C" {
@@ -154,8 +161,9 @@ uint64_t orc_unet_num_params() {
 }
 
 // One forward + backward pass of the U-Net. rad: n*h*w*3, feat: n*h*w*7 FP16
-// bits, target: n*h*w*3. out: n*h*w*3 network output (log space); grads:
-// orc_unet_num_params() doubles; returns the L1 loss.
+// bits, target: n*h*w*3. Radiance and target are divided by the albedo
+// demodulation before log1p. out: n*h*w*3 network output (log space);
+// grads: orc_unet_num_params() doubles; returns the L1 loss.
 double orc_unet(const float *params, const float *rad, const uint16_t *feat, const float *target, int n, int h,
                 int w, double *out, double *grads) {
     std::vector<Conv> cv;
@@ -167,7 +175,8 @@ double orc_unet(const float *params, const float *rad, const uint16_t *feat, con
     T x0 = make(n, h, w, 10);
     const size_t px = (size_t)n * h * w;
     for (size_t p = 0; p < px; p++) {
-        for (int k = 0; k < 3; k++) x0.v[p * 10 + k] = bf16(std::log1p((double)std::fmax(rad[3 * p + k], 0.f)));
+        for (int k = 0; k < 3; k++)
+            x0.v[p * 10 + k] = bf16(std::log1p((double)(std::fmax(rad[3 * p + k], 0.f) / demod(feat, 3 * p + k))));
         for (int k = 0; k < 7; k++) x0.v[p * 10 + 3 + k] = bf16(half_to_double(feat[7 * p + k]));
     }
     // forward
@@ -198,7 +207,7 @@ double orc_unet(const float *params, const float *rad, const uint16_t *feat, con
     double loss = 0.0;
     T gy = make(n, h, w, 3);
     for (size_t k = 0; k < nv; k++) {
-        const double diff = y.v[k] - (double)log1pf(std::fmax(target[k], 0.f));
+        const double diff = y.v[k] - (double)log1pf(std::fmax(target[k], 0.f) / demod(feat, k));
         loss += std::fabs(diff);
         gy.v[k] = (diff > 0 ? 1.0 : (diff < 0 ? -1.0 : 0.0)) / (double)nv;
     }
