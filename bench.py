@@ -17,6 +17,7 @@ rays / the slowest rank's time.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import statistics
@@ -47,7 +48,9 @@ def parse():
     ap.add_argument("--dn-train-res", type=int, default=512, help="denoise: training image size")
     ap.add_argument("--dn-cuda-cores", action="store_true", help="denoise-infer: CUDA-core convolutions")
     ap.add_argument("--dn-spp-in", type=int, default=4, help="denoise: samples per pixel of the noisy input")
-    ap.add_argument("--dn-ref-spp", type=int, default=1024, help="denoise: reference samples per pixel")
+    ap.add_argument("--dn-ref-spp", type=int, default=1024, help="denoise: training target samples per pixel")
+    ap.add_argument("--dn-eval-ref-spp", type=int, default=4096,
+                    help="denoise: samples per pixel of the held-out rooms' references")
     ap.add_argument("--scheduler", choices=["pixel", "wavefront"], default="wavefront",
                     help="room workload: path-tracing scheduler")
     ap.add_argument("--spp", type=int, default=0, help="room/batch: samples per pixel (0 = workload default)")
@@ -428,7 +431,9 @@ def run_denoise(args):
     train_seeds = list(range(cfg.seed, cfg.seed + cfg.train_rooms))
     eval_seeds = list(range(cfg.seed + 100_000, cfg.seed + 100_000 + cfg.eval_rooms))
     _, rad, feat, ref = D.make_dataset(cfg, train_seeds, torch, cfg.train_res)
-    eval_scs, _, _, eval_refs = D.make_dataset(cfg, eval_seeds, torch)
+    # held-out rooms are judged against references with more samples (the error target's yardstick)
+    eval_cfg = dataclasses.replace(cfg, spp_ref=args.dn_eval_ref_spp)
+    eval_scs, _, _, eval_refs = D.make_dataset(eval_cfg, eval_seeds, torch)
     data_s = time.perf_counter() - t0
     den = native.Denoiser(seed=cfg.seed)
     t0 = time.perf_counter()
@@ -449,7 +454,8 @@ def run_denoise(args):
     line = {"metric": "time to relMSE<=0.01, denoised / plain", "value": round(float(np.mean(td) / np.mean(tp)), 4)
             if tp else None, "unit": "ratio", "n_gpus": 1, "higher_is_better": False, "dtype": "bf16",
             "data": "synthetic", "config": {"workload": f"procedural rooms, evaluated at {cfg.res}x{cfg.res}, {cfg.spp_in} spp input,"
-                                                        f" {cfg.spp_ref} spp FP64 reference, {cfg.train_rooms} train rooms"
+                                                        f" {cfg.spp_ref} spp FP64 training targets,"
+                                                        f" {eval_cfg.spp_ref} spp FP64 evaluation references, {cfg.train_rooms} train rooms"
                                                         f" at {cfg.train_res}^2 ({cfg.crop}^2 crops, batch {cfg.batch}),"
                                                         f" {cfg.eval_rooms} held-out rooms, {cfg.steps} Adam steps"},
             "relmse_noisy_mean": float(np.mean([r["relmse_noisy"] for r in rows])),

@@ -25,7 +25,8 @@ struct TcConvPlan {
     const __nv_bfloat16 *x;
     int n, h, w, cin, cout, npad, relu;
     int tiles_x, tiles_y, tiles, splits, taps_per_split, taps_per_stage, stages, tmem_cols;
-    uint32_t w_off, bar_off;
+    int persistent, grid;  // persistent pipelined kernel (no split, weights resident) and its CTAs
+    uint32_t w_off, bar_off, halo_stride;
     size_t smem, partial_floats;
 };
 cudaError_t tc_conv_plan(TcConvPlan &p, const __nv_bfloat16 *x, int n, int h, int w, int cin, int cout, bool relu,

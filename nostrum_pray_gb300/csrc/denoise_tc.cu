@@ -48,6 +48,7 @@ constexpr uint32_t kPlaneBytes = 2944;                  // plane stride, 128-byt
 constexpr uint32_t kRowBytes = kHaloW * 16;             // one halo row of one plane (160)
 constexpr uint32_t kWaitLimit = 1u << 24;
 constexpr size_t kSmemBudget = 110 * 1024;              // target per CTA (two or more CTAs per SM)
+constexpr size_t kSmemPersistent = 200 * 1024;          // persistent kernel: up to one CTA per SM
 constexpr size_t kSmemMax = 227 * 1024;
 constexpr size_t kSmemPerSm = 228 * 1024;
 
@@ -62,6 +63,7 @@ struct TcArgs {
     int taps_per_split, taps_per_stage, stages;
     int tmem_cols;
     uint32_t w_off, bar_off;  // shared-memory offsets (the halo is at 0)
+    uint32_t halo_stride;     // persistent kernel: offset of the second halo buffer
     int *err;
 };
 
@@ -133,6 +135,58 @@ __device__ __forceinline__ void commit(uint32_t bar) {
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
     const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
     return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+// Epilogue of one tile: warp w reads TMEM lanes 32w..32w+31 (tile rows m =
+// pixel (m / 8, m % 8)) from column `tmem` on, 16 columns at a time, and
+// stores bias + ReLU + BF16 (16-byte stores), FP32, or raw FP32 partials.
+__device__ __forceinline__ void epilogue(const TcArgs &P, uint32_t tmem, int img, int y0, int x0, int split) {
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int m = warp * 32 + (tid & 31);
+    const int yy = y0 + (m >> 3), xx = x0 + (m & 7);
+    const bool valid = yy < P.h && xx < P.wd;
+    const size_t M = (size_t)P.n * P.h * P.wd;
+    const size_t pix = ((size_t)img * P.h + yy) * P.wd + xx;
+    for (int c0 = 0; c0 < P.npad; c0 += 16) {
+        uint32_t r[16];
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+            "[%16];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+              "=r"(r[15])
+            : "r"(taddr)
+            : "memory");
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (!valid) continue;
+        if (P.partial) {
+            float4 *o = reinterpret_cast<float4 *>(P.partial + ((size_t)split * M + pix) * P.npad + c0);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                o[k] = make_float4(__uint_as_float(r[4 * k]), __uint_as_float(r[4 * k + 1]),
+                                   __uint_as_float(r[4 * k + 2]), __uint_as_float(r[4 * k + 3]));
+        } else if (P.y && (P.cout & 15) == 0) {
+            float v[16];
+#pragma unroll
+            for (int k = 0; k < 16; k++) {
+                v[k] = __uint_as_float(r[k]) + __ldg(P.bias + c0 + k);
+                if (P.relu) v[k] = fmaxf(v[k], 0.f);
+            }
+            uint4 *o = reinterpret_cast<uint4 *>(P.y + pix * P.cout + c0);
+            o[0] = make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
+            o[1] = make_uint4(pack2(v[8], v[9]), pack2(v[10], v[11]), pack2(v[12], v[13]), pack2(v[14], v[15]));
+        } else {
+#pragma unroll
+            for (int k = 0; k < 16; k++) {
+                if (c0 + k >= P.cout) break;
+                float v = __uint_as_float(r[k]) + __ldg(P.bias + c0 + k);
+                if (P.relu) v = fmaxf(v, 0.f);
+                if (P.y) P.y[pix * P.cout + c0 + k] = __float2bfloat16(v);
+                if (P.y32) P.y32[pix * P.cout + c0 + k] = v;
+            }
+        }
+    }
 }
 
 __global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtensorMap xmap, TcArgs P) {
@@ -236,53 +290,155 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtenso
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     __syncthreads();
     if (!ok && tid == 0) atomicExch(P.err, 1);
-    if (ok) {
-        // warp w holds TMEM lanes 32w..32w+31 = tile rows m: pixel (m / 8, m % 8)
-        const int m = warp * 32 + (tid & 31);
-        const int yy = y0 + (m >> 3), xx = x0 + (m & 7);
-        const bool valid = yy < P.h && xx < P.wd;
-        const size_t M = (size_t)P.n * P.h * P.wd;
-        const size_t pix = ((size_t)img * P.h + yy) * P.wd + xx;
-        for (int c0 = 0; c0 < P.npad; c0 += 16) {
-            uint32_t r[16];
-            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                "[%16];"
-                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                  "=r"(r[15])
-                : "r"(taddr)
-                : "memory");
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (!valid) continue;
-            if (P.partial) {
-                float4 *o = reinterpret_cast<float4 *>(P.partial + ((size_t)split * M + pix) * P.npad + c0);
-#pragma unroll
-                for (int k = 0; k < 4; k++)
-                    o[k] = make_float4(__uint_as_float(r[4 * k]), __uint_as_float(r[4 * k + 1]),
-                                       __uint_as_float(r[4 * k + 2]), __uint_as_float(r[4 * k + 3]));
-            } else if (P.y && (P.cout & 15) == 0) {
-                float v[16];
-#pragma unroll
-                for (int k = 0; k < 16; k++) {
-                    v[k] = __uint_as_float(r[k]) + __ldg(P.bias + c0 + k);
-                    if (P.relu) v[k] = fmaxf(v[k], 0.f);
+    if (ok) epilogue(P, tmem, img, y0, x0, split);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(P.tmem_cols)
+                     : "memory");
+    }
+}
+
+// Persistent, pipelined variant for levels that need no tap split and whose
+// weights fit in shared memory next to two halos: each CTA loads the
+// weights once, then walks tiles blockIdx.x, blockIdx.x + gridDim.x, ...
+// with two halo buffers and two TMEM accumulators, so that the halo of tile
+// i + 1 is in flight and the MMAs of tile i run while the epilogue of tile
+// i - 1 drains.
+//   iteration i: thread 0 waits for halo i, issues its MMAs into
+//   accumulator i % 2 and commits them; then (i >= 1) every thread waits for
+//   the MMAs of tile i - 1, thread 0 starts the halo load of tile i + 1 into
+//   the buffer tile i - 1 used, and all warps run the epilogue of tile i - 1.
+__global__ void __launch_bounds__(128) k_conv_tc_persistent(const __grid_constant__ CUtensorMap xmap, TcArgs P) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int nchunk = P.cin >> 3;
+    const uint32_t halo0 = smem_u32(smem), wbase = halo0 + P.w_off;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + P.bar_off);
+    // bars[0..1] halo b loaded, bars[2..3] MMAs of accumulator b done,
+    // bars[4] weights loaded, bars[5] final drain
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 6);
+    int *fail = reinterpret_cast<int *>(tmem_slot + 1);
+    auto bar = [&](int i) { return smem_u32(&bars[i]); };
+    const int per_img = P.tiles_x * P.tiles_y;
+    const int tiles = P.n * per_img;
+    const int items = tiles > (int)blockIdx.x ? (tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    auto tile_of = [&](int i, int &img, int &y0, int &x0) {
+        const int t = (int)blockIdx.x + i * (int)gridDim.x;
+        img = t / per_img;
+        const int rem = t - img * per_img;
+        y0 = (rem / P.tiles_x) * kTileH;
+        x0 = (rem % P.tiles_x) * kTileW;
+    };
+    const uint32_t wbytes = (uint32_t)P.cin * P.npad * 2 * 9;
+    const int acc_stride = (P.npad + 31) & ~31;  // TMEM columns between the two accumulators
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(P.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int i = 0; i < 6; i++) mbar_init(bar(i));
+        *fail = 0;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t idesc = inst_desc(128, P.npad);
+
+    // thread 0's bookkeeping of copies issued and waited for (drained on exit)
+    int halos_issued = 0, halos_waited = 0;
+    bool w_waited = false;
+    auto load_halo = [&](int i) {
+        int img, y0, x0;
+        tile_of(i, img, y0, x0);
+        const int b = i & 1;
+        const uint32_t dst = halo0 + b * P.halo_stride;
+        mbar_expect_tx(bar(b), (uint32_t)nchunk * kChunkBytes);
+        for (int c = 0; c < nchunk; c++) tma_halo(dst + c * kPlaneBytes, &xmap, bar(b), 8 * c, x0 - 1, y0 - 1, img);
+        halos_issued = i + 1;
+    };
+    if (tid == 0 && items > 0) {
+        mbar_expect_tx(bar(4), wbytes);
+        bulk_copy(wbase, P.w, wbytes, bar(4));
+        load_halo(0);
+        if (items > 1) load_halo(1);
+        if (!mbar_wait(bar(4), 0)) *fail = 1;
+        w_waited = true;
+    }
+    __syncthreads();
+    int done = 0;  // tiles whose epilogue ran
+    for (int i = 0; i < items && !*fail; i++) {
+        const int b = i & 1;
+        if (tid == 0) {
+            if (mbar_wait(bar(b), (uint32_t)(i >> 1) & 1)) {
+                halos_waited = i + 1;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t acc = tmem + (uint32_t)(b * acc_stride);
+                const uint32_t hb = halo0 + b * P.halo_stride;
+                for (int tap = 0; tap < 9; tap++) {
+                    const int dy = tap / 3, dx = tap - 3 * (tap / 3);
+                    const uint32_t a0 = hb + (uint32_t)(dy * kHaloW + dx) * 16;
+                    const uint32_t b0 = wbase + (uint32_t)tap * P.cin * P.npad * 2;
+                    for (int p = 0; p < nchunk / 2; p++) {
+                        const uint64_t ad = smem_desc(a0 + 2 * p * kPlaneBytes, kPlaneBytes, kRowBytes);
+                        const uint64_t bd = smem_desc(b0 + 2 * p * P.npad * 16, P.npad * 16, 128);
+                        mma(acc, ad, bd, idesc, (tap | p) != 0 ? 1u : 0u);
+                    }
                 }
-                uint4 *o = reinterpret_cast<uint4 *>(P.y + pix * P.cout + c0);
-                o[0] = make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
-                o[1] = make_uint4(pack2(v[8], v[9]), pack2(v[10], v[11]), pack2(v[12], v[13]), pack2(v[14], v[15]));
             } else {
-#pragma unroll
-                for (int k = 0; k < 16; k++) {
-                    if (c0 + k >= P.cout) break;
-                    float v = __uint_as_float(r[k]) + __ldg(P.bias + c0 + k);
-                    if (P.relu) v = fmaxf(v, 0.f);
-                    if (P.y) P.y[pix * P.cout + c0 + k] = __float2bfloat16(v);
-                    if (P.y32) P.y32[pix * P.cout + c0 + k] = v;
-                }
+                *fail = 1;
             }
+            commit(bar(2 + b));
         }
+        if (i >= 1) {
+            const int j = i - 1, bj = j & 1;
+            if (!mbar_wait(bar(2 + bj), (uint32_t)(j >> 1) & 1)) atomicExch(fail, 1);
+            // the MMAs of tile j are done: its halo buffer takes tile i + 1
+            if (tid == 0 && !*fail && i + 1 < items) load_halo(i + 1);
+        }
+        __syncthreads();
+        if (*fail) break;
+        if (i >= 1) {
+            const int j = i - 1;
+            int img, y0, x0;
+            tile_of(j, img, y0, x0);
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            epilogue(P, tmem + (uint32_t)((j & 1) * acc_stride), img, y0, x0, 0);
+            done = i;
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncthreads();
+        }
+    }
+    if (!*fail && items > 0) {
+        // the last tile
+        const int j = items - 1, bj = j & 1;
+        const bool ok = mbar_wait(bar(2 + bj), (uint32_t)(j >> 1) & 1);
+        if (!ok) atomicExch(fail, 1);
+        __syncthreads();
+        if (!*fail) {
+            int img, y0, x0;
+            tile_of(j, img, y0, x0);
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            epilogue(P, tmem + (uint32_t)(bj * acc_stride), img, y0, x0, 0);
+            done = items;
+        }
+    }
+    (void)done;
+    if (tid == 0) {
+        if (*fail) {
+            atomicExch(P.err, 1);
+            // drain what is still in flight (bounded) before the shared memory goes away
+            if (!w_waited && items > 0) mbar_wait(bar(4), 0);
+            for (int i = halos_waited; i < halos_issued; i++) mbar_wait(bar(i & 1), (uint32_t)(i >> 1) & 1);
+        }
+        commit(bar(5));
+        mbar_wait(bar(5), 0);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -294,30 +450,42 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtenso
 }
 
 // Sum of the split partials in split order, plus bias, ReLU, store; four
-// channels per thread (cout a multiple of 4).
+// channels per thread when cout is a multiple of 4, else one.
+template <int kVec>
 __global__ void k_conv_finalize(const float *partial, const float *bias, __nv_bfloat16 *y, float *y32, size_t M,
                                 int npad, int cout, int splits, int relu) {
-    const int groups = cout / 4;
+    const int groups = cout / kVec;
     const size_t total = M * (size_t)groups;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         const size_t pix = i / groups;
-        const int co = 4 * (int)(i - pix * groups);
-        float4 s = *reinterpret_cast<const float4 *>(partial + pix * npad + co);
-        for (int k = 1; k < splits; k++) {
-            const float4 q = *reinterpret_cast<const float4 *>(partial + ((size_t)k * M + pix) * npad + co);
-            s.x = s.x + q.x, s.y = s.y + q.y, s.z = s.z + q.z, s.w = s.w + q.w;
+        const int co = kVec * (int)(i - pix * groups);
+        float v[kVec];
+#pragma unroll
+        for (int k = 0; k < kVec; k++) v[k] = partial[pix * npad + co + k];
+        for (int s = 1; s < splits; s++) {
+            const float *q = partial + ((size_t)s * M + pix) * npad + co;
+#pragma unroll
+            for (int k = 0; k < kVec; k++) v[k] = v[k] + q[k];
         }
-        const float4 b = *reinterpret_cast<const float4 *>(bias + co);
-        float v[4] = {s.x + b.x, s.y + b.y, s.z + b.z, s.w + b.w};
-        if (relu)
-            for (int k = 0; k < 4; k++) v[k] = fmaxf(v[k], 0.f);
-        if (y) {
-            uint2 o;
-            o.x = pack2(v[0], v[1]);
-            o.y = pack2(v[2], v[3]);
-            *reinterpret_cast<uint2 *>(y + pix * cout + co) = o;
+#pragma unroll
+        for (int k = 0; k < kVec; k++) {
+            v[k] = v[k] + bias[co + k];
+            if (relu) v[k] = fmaxf(v[k], 0.f);
         }
-        if (y32) *reinterpret_cast<float4 *>(y32 + pix * cout + co) = make_float4(v[0], v[1], v[2], v[3]);
+        if (kVec == 4) {
+            if (y) {
+                uint2 o;
+                o.x = pack2(v[0], v[1 % kVec]);
+                o.y = pack2(v[2 % kVec], v[3 % kVec]);
+                *reinterpret_cast<uint2 *>(y + pix * cout + co) = o;
+            }
+            if (y32)
+                *reinterpret_cast<float4 *>(y32 + pix * cout + co) =
+                    make_float4(v[0], v[1 % kVec], v[2 % kVec], v[3 % kVec]);
+        } else {
+            if (y) y[pix * cout + co] = __float2bfloat16(v[0]);
+            if (y32) y32[pix * cout + co] = v[0];
+        }
     }
 }
 
@@ -397,18 +565,39 @@ cudaError_t tc_conv_plan(TcConvPlan &p, const __nv_bfloat16 *x, int n, int h, in
         if (fit < 2) fit = 2;
         p.stages = (int)(fit < (size_t)p.taps_per_split ? fit : (size_t)p.taps_per_split);
     }
-    p.w_off = (uint32_t)halo;
-    p.bar_off = (uint32_t)(halo + (size_t)p.stages * p.taps_per_stage * wtap);
-    p.bar_off = (p.bar_off + 15) & ~15u;
-    size_t smem = p.bar_off + 8 * (2 + 2 * (size_t)p.stages) + 16;
+    // persistent pipelined kernel: no split, two halos and all weights resident
+    p.persistent = p.splits == 1 && 2 * halo + 9 * wtap + 64 <= kSmemPersistent;
+    size_t smem;
     int cols = 32;
-    while (cols < p.npad) cols <<= 1;
+    if (p.persistent) {
+        p.halo_stride = (uint32_t)halo;
+        p.w_off = (uint32_t)(2 * halo);
+        p.bar_off = (uint32_t)((2 * halo + 9 * wtap + 15) & ~(size_t)15);
+        smem = p.bar_off + 8 * 6 + 16;
+        while (cols < 2 * ((p.npad + 31) & ~31)) cols <<= 1;
+    } else {
+        p.halo_stride = 0;
+        p.w_off = (uint32_t)halo;
+        p.bar_off = (uint32_t)(halo + (size_t)p.stages * p.taps_per_stage * wtap);
+        p.bar_off = (p.bar_off + 15) & ~15u;
+        smem = p.bar_off + 8 * (2 + 2 * (size_t)p.stages) + 16;
+        while (cols < p.npad) cols <<= 1;
+    }
     p.tmem_cols = cols;
     // no more CTAs per SM than TMEM has columns for (tcgen05.alloc would wait)
     const size_t max_ctas = 512 / cols;
     if (kSmemPerSm / (smem + 1024) > max_ctas) smem = kSmemPerSm / max_ctas - 1024 + 16;
     if (smem > kSmemMax) return cudaErrorInvalidValue;
     p.smem = smem;
+    if (p.persistent) {
+        size_t per_sm = kSmemPerSm / (smem + 1024);
+        if (per_sm > max_ctas) per_sm = max_ctas;
+        if (per_sm < 1) per_sm = 1;
+        const long long slots = (long long)sm_count * (long long)per_sm;
+        p.grid = (int)(tiles < slots ? tiles : slots);
+    } else {
+        p.grid = p.tiles;
+    }
     p.partial_floats = p.splits > 1 ? (size_t)p.splits * n * h * w * p.npad : 0;
 
     EncodeTiled enc = encode_fn();
@@ -426,10 +615,12 @@ cudaError_t tc_conv_plan(TcConvPlan &p, const __nv_bfloat16 *x, int n, int h, in
 
 cudaError_t conv3x3_forward_tc(const TcConvPlan &p, const __nv_bfloat16 *wpacked, const float *bias,
                                __nv_bfloat16 *y, float *y32, float *partial, int *err, cudaStream_t st) {
-    if (p.splits > 1 && (!partial || (p.cout & 3))) return cudaErrorInvalidValue;
+    if (p.splits > 1 && !partial) return cudaErrorInvalidValue;
     static bool attr_set = false;
     if (!attr_set) {
         cudaError_t e = cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_conv_tc_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
@@ -442,16 +633,23 @@ cudaError_t conv3x3_forward_tc(const TcConvPlan &p, const __nv_bfloat16 *wpacked
     a.tiles_x = p.tiles_x, a.tiles_y = p.tiles_y;
     a.taps_per_split = p.taps_per_split, a.taps_per_stage = p.taps_per_stage, a.stages = p.stages;
     a.tmem_cols = p.tmem_cols;
-    a.w_off = p.w_off, a.bar_off = p.bar_off;
+    a.w_off = p.w_off, a.bar_off = p.bar_off, a.halo_stride = p.halo_stride;
     a.err = err;
     CUtensorMap map;
     std::memcpy(&map, p.tmap, sizeof(map));
-    k_conv_tc<<<dim3((unsigned)p.tiles, (unsigned)p.splits), 128, p.smem, st>>>(map, a);
+    if (p.persistent)
+        k_conv_tc_persistent<<<(unsigned)p.grid, 128, p.smem, st>>>(map, a);
+    else
+        k_conv_tc<<<dim3((unsigned)p.tiles, (unsigned)p.splits), 128, p.smem, st>>>(map, a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || p.splits == 1) return e;
     const size_t M = (size_t)p.n * p.h * p.w;
-    k_conv_finalize<<<grid_for(M * p.cout / 4), 256, 0, st>>>(partial, bias, y, y32, M, p.npad, p.cout, p.splits,
-                                                               p.relu);
+    if ((p.cout & 3) == 0)
+        k_conv_finalize<4><<<grid_for(M * p.cout / 4), 256, 0, st>>>(partial, bias, y, y32, M, p.npad, p.cout,
+                                                                      p.splits, p.relu);
+    else
+        k_conv_finalize<1><<<grid_for(M * p.cout), 256, 0, st>>>(partial, bias, y, y32, M, p.npad, p.cout, p.splits,
+                                                                  p.relu);
     return cudaGetLastError();
 }
 

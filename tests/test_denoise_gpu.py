@@ -34,13 +34,26 @@ def random_batch(seed, n, h, w):
     return rad, feat, tgt
 
 
-def test_gradients_match_fp64_oracle(oracle):
+# resolution level of each convolution (size >> level)
+LEVELS = [0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 3, 3, 2, 2, 1, 1, 0, 0, 0]
+
+
+@pytest.mark.parametrize("tensor_cores", [True, False])
+def test_gradients_match_fp64_oracle(oracle, tensor_cores):
+    """Loss, output and every parameter's gradient against the FP64 oracle
+    (which rounds stored activations to BF16 at the same points), with the
+    forward pass on the tensor cores and on the CUDA cores. Tolerances: the
+    gradient vector as a whole within 2 %; each convolution's weights within
+    3 % at levels 0-2 and 8 % at levels 3-4 (8 x 8 and 4 x 4 pixels here),
+    where a BF16 rounding flip of one stored activation (or of a ReLU sign)
+    weighs more: measured 2-5 % there on both paths."""
     den = native.Denoiser(seed=5)
+    den.set_tensor_cores(tensor_cores)
     params = den.get_params()
-    rad, feat, tgt = random_batch(1, 2, 32, 32)
+    rad, feat, tgt = random_batch(1, 2, 64, 64)
     t = lambda a: torch.from_numpy(a).cuda()
     loss, g = den.gradients(t(rad), t(feat), t(tgt))
-    out = torch.empty((2, 32, 32, 3), dtype=torch.float32, device="cuda")
+    out = torch.empty((2, 64, 64, 3), dtype=torch.float32, device="cuda")
     den.denoise(t(rad), t(feat), out)
     torch.cuda.synchronize()
     oloss, oout, og = oracle.unet(params, rad, feat, tgt)
@@ -48,11 +61,13 @@ def test_gradients_match_fp64_oracle(oracle):
     # the output is re-modulated by the albedo; the oracle returns the network output in log space
     dm = (np.maximum(feat[..., 0:3].astype(np.float32), 0) + np.float32(0.05)).astype(np.float64)
     assert rel(np.log1p(out.cpu().numpy().astype(np.float64) / dm), oout) < 5e-3
+    assert rel(g, og) < 2e-2
     off = 0
-    for cin, cout in CONVS:
+    for (cin, cout), level in zip(CONVS, LEVELS):
         nw = cout * 9 * cin
-        assert rel(g[off:off + nw], og[off:off + nw]) < 3e-2, (cin, cout)
-        assert rel(g[off + nw:off + nw + cout], og[off + nw:off + nw + cout]) < 3e-2, (cin, cout, "bias")
+        tol = 3e-2 if level <= 2 else 8e-2
+        assert rel(g[off:off + nw], og[off:off + nw]) < tol, (cin, cout)
+        assert rel(g[off + nw:off + nw + cout], og[off + nw:off + nw + cout]) < tol, (cin, cout, "bias")
         off += nw + cout
     assert off == den.num_params
 
@@ -90,14 +105,16 @@ def test_features_match_oracle_hits(oracle):
     np.testing.assert_array_equal(got, want.astype(np.float16))
 
 
-@pytest.mark.parametrize("shape", [(1, 16, 16), (2, 48, 32), (2, 80, 48), (1, 256, 256)])
+@pytest.mark.parametrize("shape", [(1, 16, 16), (2, 48, 32), (2, 80, 48), (2, 256, 256), (1, 512, 512)])
 def test_tensor_core_forward_matches_cuda_cores(shape):
     """The tcgen05 implicit-GEMM convolutions give the CUDA-core result (same
     BF16 operands, FP32 accumulation; only the summation order differs).
     Shapes cover partial tiles (80 x 48 and 16 x 16 down to 5 x 3 and 1 x 1
-    at the deepest level), two images, and all three tap splits (1 at 256^2,
-    3 at 128^2, 9 below). Compared: the network's correction (output minus
-    input in log space), which every convolution feeds."""
+    at the deepest level), two images, all three tap splits (1 from 304
+    tiles up, 3 from 102, 9 below) and the persistent pipelined kernel (the
+    unsplit levels of 256^2 and 512^2 frames). Compared: the network's
+    correction (output minus input in log space), which every convolution
+    feeds."""
     n, h, w = shape
     den = native.Denoiser(seed=9)
     rad, feat, _ = random_batch(4, n, h, w)
