@@ -57,7 +57,7 @@ struct WavefrontScratch {
     int32_t *hit_ref;                // per path: closest-hit reference (-1: miss)
     uint32_t *queue[2];              // path ids, ping-pong
     float4 *shadow;                  // occlusion jobs: 3 float4 each (origin+path, dir+dist2, contribution)
-    uint32_t *counts;                // [0], [1]: queue lengths, [2]: occlusion jobs
+    uint32_t *counts;                // [0], [1]: queue lengths, [2]: occlusion jobs, [3], [4]: fetch counters
     float *pixel_sum;                // per pixel x 3: running float sum over samples
     uint64_t capacity;               // paths per round
 };

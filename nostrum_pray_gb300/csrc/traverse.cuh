@@ -141,111 +141,134 @@ __device__ __forceinline__ bool pop_node(const uint32_t *stk_a, const uint32_t *
 // postponed leaves together, so lanes do the same kind of work at the same
 // time.
 //
-// Closest hit (kAny = false): returns the index of the winning triangle
-// record or -1, its distance in best_t.
-// Any hit (kAny = true): returns >= 0 once a triangle with t > 0 and
-// t * t < d2 is found (the occlusion test of src/pray.cpp:42).
-template <bool kAny, bool kCount = false, int kStackN = kStack>
-__device__ __forceinline__ int traverse(const DevScene &s, const RayF &r, float eps, float d2, bool valid,
-                                        float &best_t, FetchCount *fc = nullptr) {
-    static_assert(kStackN >= 2 && kStackN <= kStack, "stack entries");
-    constexpr unsigned kFull = 0xFFFFFFFFu;
-    best_t = FLT_MAX;
-    int best = -1;
-    uint32_t best_key = 0xFFFFFFFFu;
-    float limit = kAny ? sqrtf(d2) * kPruneRel : FLT_MAX;
-    const float back = -s.tol;
-    uint32_t a = 0, b = 0, la = 0, lb = 0;
-    float cur_tn = 0.f, leaf_tn = 0.f;
-    bool have_node = false, have_leaf = false;
-    const bool finite = isfinite(r.ix) && isfinite(r.iy) && isfinite(r.iz);
+// The per-lane state lives in Trav, so that a kernel can also run the
+// traversal round by round and hand a lane whose ray is done a new ray
+// (dynamic fetch): trav_start tests the root, trav_round runs one interior
+// phase and one leaf phase for the whole warp, and a lane is done when
+// active() turns false.
+//
+// Closest hit (kAny = false): best = index of the winning triangle record or
+// -1, its distance in best_t. Any hit (kAny = true): best >= 0 once a
+// triangle with t > 0 and t * t < d2 is found (the occlusion test of
+// src/pray.cpp:42).
+struct Trav {
+    uint32_t a, b, la, lb;
+    float cur_tn, leaf_tn, limit, back, best_t;
+    int best, sp;
+    uint32_t best_key;
+    bool have_node, have_leaf, finite;
+    __device__ __forceinline__ bool active() const { return have_node || have_leaf; }
+};
+
+// The traversal stack of one lane (kept apart from Trav so that the scalar
+// state stays in registers).
+template <int kStackN>
+struct TravStack {
+    uint32_t a[kStackN], b[kStackN];
+    float t[kStackN];
+};
+
+template <bool kAny>
+__device__ __forceinline__ void trav_start(const DevScene &s, const RayF &r, float d2, bool valid, Trav &T) {
+    T.best_t = FLT_MAX;
+    T.best = -1;
+    T.best_key = 0xFFFFFFFFu;
+    T.limit = kAny ? sqrtf(d2) * kPruneRel : FLT_MAX;
+    T.back = -s.tol;
+    T.a = T.b = T.la = T.lb = 0;
+    T.cur_tn = T.leaf_tn = 0.f;
+    T.have_node = T.have_leaf = false;
+    T.sp = 0;
+    T.finite = isfinite(r.ix) && isfinite(r.iy) && isfinite(r.iz);
     if (valid) {
         float tn, tf;
         const float4 rlo = ldg4(s.nodes[0].lo), rhi = ldg4(s.nodes[0].hi);
         if (slab(rlo, rhi, r, tn, tf)) {
-            a = __float_as_uint(rlo.w);
-            b = __float_as_uint(rhi.w);
-            cur_tn = tn;
-            have_node = true;
+            T.a = __float_as_uint(rlo.w);
+            T.b = __float_as_uint(rhi.w);
+            T.cur_tn = tn;
+            T.have_node = true;
         }
     }
-    uint32_t stk_a[kStackN], stk_b[kStackN];
-    float stk_t[kStackN];
-    int sp = 0;
-    while (__any_sync(kFull, have_node || have_leaf)) {
-        // 1. interior nodes, until every lane has found a leaf
-        while (true) {
-            const bool interior = have_node && !(b & kLeafFlag);
-            if (!__any_sync(kFull, interior && !have_leaf)) break;
-            if (interior) {
-                if (kCount) fc->pairs++;
-                const GNode *c = s.nodes + a;
-                const float4 l0 = ldg4(c[0].lo), h0 = ldg4(c[0].hi), l1 = ldg4(c[1].lo), h1 = ldg4(c[1].hi);
-                float tn0, tf0, tn1, tf1;
-                const bool v0 = slab(l0, h0, r, finite, tn0, tf0) && tn0 <= limit && tf0 >= back;
-                const bool v1 = slab(l1, h1, r, finite, tn1, tf1) && tn1 <= limit && tf1 >= back;
-                if (v0 && v1) {
-                    const bool first0 = tn0 <= tn1;
-                    stk_a[sp] = __float_as_uint(first0 ? l1.w : l0.w);
-                    stk_b[sp] = __float_as_uint(first0 ? h1.w : h0.w);
-                    stk_t[sp] = first0 ? tn1 : tn0;
-                    sp++;
-                    a = __float_as_uint(first0 ? l0.w : l1.w);
-                    b = __float_as_uint(first0 ? h0.w : h1.w);
-                    cur_tn = first0 ? tn0 : tn1;
-                } else if (v0 || v1) {
-                    a = __float_as_uint(v0 ? l0.w : l1.w);
-                    b = __float_as_uint(v0 ? h0.w : h1.w);
-                    cur_tn = v0 ? tn0 : tn1;
-                } else {
-                    have_node = pop_node(stk_a, stk_b, stk_t, sp, limit, a, b, cur_tn);
-                }
-                if (have_node && (b & kLeafFlag) && !have_leaf) {
-                    // first leaf: postpone it and keep walking
-                    la = a, lb = b, leaf_tn = cur_tn;
-                    have_leaf = true;
-                    have_node = pop_node(stk_a, stk_b, stk_t, sp, limit, a, b, cur_tn);
-                }
+}
+
+template <bool kAny, bool kCount, int kStackN>
+__device__ __forceinline__ void trav_round(const DevScene &s, const RayF &r, float eps, float d2, Trav &T,
+                                           TravStack<kStackN> &S, FetchCount *fc) {
+    static_assert(kStackN >= 2 && kStackN <= kStack, "stack entries");
+    constexpr unsigned kFull = 0xFFFFFFFFu;
+    // 1. interior nodes, until every lane has found a leaf
+    while (true) {
+        const bool interior = T.have_node && !(T.b & kLeafFlag);
+        if (!__any_sync(kFull, interior && !T.have_leaf)) break;
+        if (interior) {
+            if (kCount) fc->pairs++;
+            const GNode *c = s.nodes + T.a;
+            const float4 l0 = ldg4(c[0].lo), h0 = ldg4(c[0].hi), l1 = ldg4(c[1].lo), h1 = ldg4(c[1].hi);
+            float tn0, tf0, tn1, tf1;
+            const bool v0 = slab(l0, h0, r, T.finite, tn0, tf0) && tn0 <= T.limit && tf0 >= T.back;
+            const bool v1 = slab(l1, h1, r, T.finite, tn1, tf1) && tn1 <= T.limit && tf1 >= T.back;
+            if (v0 && v1) {
+                const bool first0 = tn0 <= tn1;
+                S.a[T.sp] = __float_as_uint(first0 ? l1.w : l0.w);
+                S.b[T.sp] = __float_as_uint(first0 ? h1.w : h0.w);
+                S.t[T.sp] = first0 ? tn1 : tn0;
+                T.sp++;
+                T.a = __float_as_uint(first0 ? l0.w : l1.w);
+                T.b = __float_as_uint(first0 ? h0.w : h1.w);
+                T.cur_tn = first0 ? tn0 : tn1;
+            } else if (v0 || v1) {
+                T.a = __float_as_uint(v0 ? l0.w : l1.w);
+                T.b = __float_as_uint(v0 ? h0.w : h1.w);
+                T.cur_tn = v0 ? tn0 : tn1;
+            } else {
+                T.have_node = pop_node(S.a, S.b, S.t, T.sp, T.limit, T.a, T.b, T.cur_tn);
+            }
+            if (T.have_node && (T.b & kLeafFlag) && !T.have_leaf) {
+                // first leaf: postpone it and keep walking
+                T.la = T.a, T.lb = T.b, T.leaf_tn = T.cur_tn;
+                T.have_leaf = true;
+                T.have_node = pop_node(S.a, S.b, S.t, T.sp, T.limit, T.a, T.b, T.cur_tn);
             }
         }
-        // 2. leaves: the postponed one, then any leaf the walk stopped on
-        while (true) {
-            const bool work = have_leaf || (have_node && (b & kLeafFlag));
-            if (!__any_sync(kFull, work)) break;
-            if (work) {
-                uint32_t fa, fb;
-                float ftn;
-                if (have_leaf) {
-                    fa = la, fb = lb, ftn = leaf_tn;
-                    have_leaf = false;
-                } else {
-                    fa = a, fb = b, ftn = cur_tn;
-                    have_node = pop_node(stk_a, stk_b, stk_t, sp, limit, a, b, cur_tn);
-                }
-                if (ftn <= limit) {
-                    const uint32_t end = fa + (fb & ~kLeafFlag);
-                    for (uint32_t i = fa; i < end; i++) {
-                        if (kCount) fc->tris++;
-                        const GTri *T = s.tris + i;
-                        const float4 v0 = ldg4(T->v0), e1 = ldg4(T->e1), e2 = ldg4(T->e2);
-                        float t;
-                        if (intersect_tri(v0, e1, e2, r, eps, t) && t > 0) {
-                            if (kAny) {
-                                if (d2 > t * t) {
-                                    best = (int)i;
-                                    have_node = have_leaf = false;
-                                    sp = 0;
-                                    break;
-                                }
-                            } else {
-                                // depth-first position in the reference's leaf order
-                                const uint32_t key = __float_as_uint(e1.w);
-                                if (t < best_t || (best >= 0 && t == best_t && key < best_key)) {
-                                    best_t = t;
-                                    best = (int)i;
-                                    best_key = key;
-                                    limit = t * kPruneRel;
-                                }
+    }
+    // 2. leaves: the postponed one, then any leaf the walk stopped on
+    while (true) {
+        const bool work = T.have_leaf || (T.have_node && (T.b & kLeafFlag));
+        if (!__any_sync(kFull, work)) break;
+        if (work) {
+            uint32_t fa, fb;
+            float ftn;
+            if (T.have_leaf) {
+                fa = T.la, fb = T.lb, ftn = T.leaf_tn;
+                T.have_leaf = false;
+            } else {
+                fa = T.a, fb = T.b, ftn = T.cur_tn;
+                T.have_node = pop_node(S.a, S.b, S.t, T.sp, T.limit, T.a, T.b, T.cur_tn);
+            }
+            if (ftn <= T.limit) {
+                const uint32_t end = fa + (fb & ~kLeafFlag);
+                for (uint32_t i = fa; i < end; i++) {
+                    if (kCount) fc->tris++;
+                    const GTri *Tr = s.tris + i;
+                    const float4 v0 = ldg4(Tr->v0), e1 = ldg4(Tr->e1), e2 = ldg4(Tr->e2);
+                    float t;
+                    if (intersect_tri(v0, e1, e2, r, eps, t) && t > 0) {
+                        if (kAny) {
+                            if (d2 > t * t) {
+                                T.best = (int)i;
+                                T.have_node = T.have_leaf = false;
+                                T.sp = 0;
+                                break;
+                            }
+                        } else {
+                            // depth-first position in the reference's leaf order
+                            const uint32_t key = __float_as_uint(e1.w);
+                            if (t < T.best_t || (T.best >= 0 && t == T.best_t && key < T.best_key)) {
+                                T.best_t = t;
+                                T.best = (int)i;
+                                T.best_key = key;
+                                T.limit = t * kPruneRel;
                             }
                         }
                     }
@@ -253,7 +276,17 @@ __device__ __forceinline__ int traverse(const DevScene &s, const RayF &r, float 
             }
         }
     }
-    return best;
+}
+
+template <bool kAny, bool kCount = false, int kStackN = kStack>
+__device__ __forceinline__ int traverse(const DevScene &s, const RayF &r, float eps, float d2, bool valid,
+                                        float &best_t, FetchCount *fc = nullptr) {
+    Trav T;
+    TravStack<kStackN> S;
+    trav_start<kAny>(s, r, d2, valid, T);
+    while (__any_sync(0xFFFFFFFFu, T.active())) trav_round<kAny, kCount>(s, r, eps, d2, T, S, fc);
+    best_t = T.best_t;
+    return T.best;
 }
 
 // Primary ray of pixel (px, py), src/scene_preprocessor.cpp:124-134.

@@ -41,6 +41,7 @@ using namespace dev;
 constexpr float kInvPi = 0.318309886183790671538f;
 constexpr float kShadowShrink = 0.999f;
 constexpr int kThreads = 256;
+constexpr int kRefillIdle = 8;  // dynamic fetch: refill a warp's idle lanes once this many are idle
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
@@ -79,6 +80,8 @@ __global__ void __launch_bounds__(kThreads) k_wf_init(PtLaunch L, WavefrontScrat
         w.counts[0] = (uint32_t)n;
         w.counts[1] = 0;
         w.counts[2] = 0;
+        w.counts[3] = 0;
+        w.counts[4] = 0;
     }
     for (uint64_t i = first_index(); i < n; i += grid_stride()) {
         const uint64_t pixel = i % P;
@@ -95,30 +98,61 @@ __global__ void __launch_bounds__(kThreads) k_wf_init(PtLaunch L, WavefrontScrat
     }
 }
 
+// Hands the warp's idle lanes (mask `idle`) the next entries of a work list
+// of n items through the counter; returns the lane's item index (>= n: none)
+// and sets `drained` (warp-uniform) once every item has been handed out.
+__device__ __forceinline__ uint32_t warp_fetch(uint32_t *counter, unsigned idle, uint32_t n, bool &drained) {
+    uint32_t base = 0;
+    if (lane_id() == 0) base = atomicAdd(counter, (uint32_t)__popc(idle));
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if ((uint64_t)base + (uint32_t)__popc(idle) >= n) drained = true;
+    return base + (uint32_t)__popc(idle & ((1u << lane_id()) - 1u));
+}
+
+// Closest hit of every queued path, with dynamic fetch (after Aila & Laine
+// 2009): each warp runs the traversal round by round and, whenever at least
+// kRefillIdle of its lanes have finished their ray, gives those lanes the next
+// queue entries (one atomic per warp), so lanes do not idle until the
+// slowest ray of the warp is done. Work is handed out through counts[3]
+// (reset by the shade pass); counts[4], the occlusion pass's counter, is
+// reset here.
+template <int kStackN>
 __global__ void __launch_bounds__(kThreads) k_wf_extend(DevScene s, PtLaunch L, WavefrontScratch w, int in, int out) {
+    constexpr unsigned kFull = 0xFFFFFFFFu;
     const uint32_t n = w.counts[in];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         w.counts[out] = 0;
         w.counts[2] = 0;
+        w.counts[4] = 0;
     }
     uint32_t seg = 0;
-    for (uint64_t i = first_index(); i < rounded(n); i += grid_stride()) {
-        const bool valid = i < n;
-        uint32_t p = 0;
-        RayF r{};
-        if (valid) {
-            p = w.queue[in][i];
-            const float4 o = w.org[p], d = w.dir[p];
-            r.ox = o.x, r.oy = o.y, r.oz = o.z;
-            r.dx = d.x, r.dy = d.y, r.dz = d.z;
-            r.ix = 1.0f / d.x, r.iy = 1.0f / d.y, r.iz = 1.0f / d.z;
+    Trav T;
+    TravStack<kStackN> S;
+    T.have_node = T.have_leaf = false;
+    RayF r{};
+    uint32_t p = 0;
+    bool has = false, drained = false;
+    while (true) {
+        const unsigned idle = __ballot_sync(kFull, !has);
+        if (!drained && (__popc(idle) >= kRefillIdle || idle == kFull)) {
+            const uint32_t idx = warp_fetch(w.counts + 3, idle, n, drained);
+            if (!has && idx < n) {
+                p = w.queue[in][idx];
+                const float4 o = w.org[p], d = w.dir[p];
+                r.ox = o.x, r.oy = o.y, r.oz = o.z;
+                r.dx = d.x, r.dy = d.y, r.dz = d.z;
+                r.ix = 1.0f / d.x, r.iy = 1.0f / d.y, r.iz = 1.0f / d.z;
+                has = true;
+                trav_start<false>(s, r, 0.f, s.n_refs > 0, T);
+            }
         }
-        float t;
-        const int pos = traverse<false>(s, r, L.eps, 0.f, valid && s.n_refs > 0, t);
-        if (valid) {
-            w.hit_t[p] = t;
-            w.hit_ref[p] = pos;
+        if (!__any_sync(kFull, has)) break;
+        trav_round<false, false>(s, r, L.eps, 0.f, T, S, nullptr);
+        if (has && !T.active()) {
+            w.hit_t[p] = T.best_t;
+            w.hit_ref[p] = T.best;
             seg++;
+            has = false;
         }
     }
     if (L.counters) warp_count(L.counters + 1, seg);
@@ -127,6 +161,7 @@ __global__ void __launch_bounds__(kThreads) k_wf_extend(DevScene s, PtLaunch L, 
 __global__ void __launch_bounds__(kThreads) k_wf_shade(DevScene s, PtLaunch L, WavefrontScratch w, int in, int out,
                                                        uint32_t round_base, uint64_t P) {
     const uint32_t n = w.counts[in];
+    if (blockIdx.x == 0 && threadIdx.x == 0) w.counts[3] = 0;  // the next extend pass's fetch counter
     for (uint64_t i = first_index(); i < rounded(n); i += grid_stride()) {
         bool cont = false, job = false;
         uint32_t p = 0;
@@ -224,27 +259,46 @@ __global__ void __launch_bounds__(kThreads) k_wf_shade(DevScene s, PtLaunch L, W
     }
 }
 
+// Any-hit test of every occlusion job, with the same dynamic fetch
+// (counts[4]); an unoccluded job adds its contribution to its path.
+template <int kStackN>
 __global__ void __launch_bounds__(kThreads) k_wf_occlude(DevScene s, PtLaunch L, WavefrontScratch w) {
+    constexpr unsigned kFull = 0xFFFFFFFFu;
     const uint32_t n = w.counts[2];
     uint32_t seg = 0;
-    for (uint64_t i = first_index(); i < rounded(n); i += grid_stride()) {
-        const bool valid = i < n;
-        float4 jo = make_float4(0.f, 0.f, 0.f, 0.f), jd = make_float4(1.f, 0.f, 0.f, 0.f), jc = jo;
-        if (valid) {
-            const float4 *j = w.shadow + 3ull * i;
-            jo = j[0], jd = j[1], jc = j[2];
+    Trav T;
+    TravStack<kStackN> S;
+    T.have_node = T.have_leaf = false;
+    RayF r{};
+    float d2 = 0.f;
+    float4 jo = make_float4(0.f, 0.f, 0.f, 0.f), jc = jo;
+    bool has = false, drained = false;
+    while (true) {
+        const unsigned idle = __ballot_sync(kFull, !has);
+        if (!drained && (__popc(idle) >= kRefillIdle || idle == kFull)) {
+            const uint32_t idx = warp_fetch(w.counts + 4, idle, n, drained);
+            if (!has && idx < n) {
+                const float4 *j = w.shadow + 3ull * idx;
+                jo = j[0];
+                const float4 jd = j[1];
+                jc = j[2];
+                r = make_ray(jo.x, jo.y, jo.z, jd.x, jd.y, jd.z);
+                d2 = jd.w;
+                has = true;
+                trav_start<true>(s, r, d2, s.n_refs > 0, T);
+            }
         }
-        const RayF r = make_ray(jo.x, jo.y, jo.z, jd.x, jd.y, jd.z);
-        float dummy;
-        const bool occluded = traverse<true>(s, r, L.eps, jd.w, valid, dummy) >= 0;
-        if (valid) {
+        if (!__any_sync(kFull, has)) break;
+        trav_round<true, false>(s, r, L.eps, d2, T, S, nullptr);
+        if (has && !T.active()) {
             seg++;
-            if (!occluded) {
+            if (T.best < 0) {
                 const uint32_t p = __float_as_uint(jo.w);
                 float4 R = w.rad[p];
                 R.x = R.x + jc.x, R.y = R.y + jc.y, R.z = R.z + jc.z;
                 w.rad[p] = R;
             }
+            has = false;
         }
     }
     if (L.counters) warp_count(L.counters + 1, seg);
@@ -306,7 +360,7 @@ __global__ void __launch_bounds__(1024) k_relmse(const double *img, double a, co
 uint64_t wavefront_scratch_bytes(uint64_t capacity, uint64_t pixels) {
     auto al = [](uint64_t b) { return (b + 255) & ~255ull; };
     return 4 * al(16 * capacity) + al(8 * capacity) + al(4 * capacity) * 3 + 2 * al(4 * capacity) +
-           al(48 * capacity) + al(16) + al(12 * pixels);
+           al(48 * capacity) + al(32) + al(12 * pixels);
 }
 
 WavefrontScratch wavefront_carve(void *base, uint64_t capacity, uint64_t pixels) {
@@ -329,7 +383,7 @@ WavefrontScratch wavefront_carve(void *base, uint64_t capacity, uint64_t pixels)
     w.queue[0] = reinterpret_cast<uint32_t *>(take(4 * capacity));
     w.queue[1] = reinterpret_cast<uint32_t *>(take(4 * capacity));
     w.shadow = reinterpret_cast<float4 *>(take(48 * capacity));
-    w.counts = reinterpret_cast<uint32_t *>(take(16));
+    w.counts = reinterpret_cast<uint32_t *>(take(32));
     w.pixel_sum = reinterpret_cast<float *>(take(12 * pixels));
     w.capacity = capacity;
     return w;
@@ -341,14 +395,17 @@ cudaError_t record_wavefront_frame(const DevScene &s, const PtLaunch &L, const W
     if (P == 0 || L.num_samples == 0) return cudaSuccess;
     const uint32_t S = (uint32_t)std::min<uint64_t>(L.num_samples, std::max<uint64_t>(1, w.capacity / P));
     const unsigned grid = (unsigned)std::max(1, sm_count) * 4;
+    const bool small_stack = s.depth < 32;  // a 32-entry traversal stack suffices
     for (uint32_t base = 0; base < L.num_samples; base += S) {
         const uint32_t Sr = std::min(S, L.num_samples - base);
         k_wf_init<<<grid, kThreads, 0, stream>>>(L, w, base, Sr, P);
         for (uint32_t it = 0; it <= L.max_depth; it++) {
             const int in = (int)(it & 1), out = 1 - in;
-            k_wf_extend<<<grid, kThreads, 0, stream>>>(s, L, w, in, out);
+            if (small_stack) k_wf_extend<32><<<grid, kThreads, 0, stream>>>(s, L, w, in, out);
+            else k_wf_extend<kStack><<<grid, kThreads, 0, stream>>>(s, L, w, in, out);
             k_wf_shade<<<grid, kThreads, 0, stream>>>(s, L, w, in, out, base, P);
-            k_wf_occlude<<<grid, kThreads, 0, stream>>>(s, L, w);
+            if (small_stack) k_wf_occlude<32><<<grid, kThreads, 0, stream>>>(s, L, w);
+            else k_wf_occlude<kStack><<<grid, kThreads, 0, stream>>>(s, L, w);
         }
         k_wf_accumulate<<<grid, kThreads, 0, stream>>>(L, w, Sr, P, base == 0 ? 1 : 0);
     }
