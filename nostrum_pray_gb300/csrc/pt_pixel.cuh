@@ -53,9 +53,12 @@ __device__ __forceinline__ uint32_t pick_emitter(const DevScene &s, float u) {
     return lo;
 }
 
-// Every lane of a warp runs the same sample loop and bounce iterations (a
-// finished path idles until the warp's last path ends) so that the
-// warp-collective traversals line up.
+// All lanes of a warp call pt_pixel together (the traversals inside are
+// warp-collective). Each lane works through its own pixel's samples in order,
+// and starts its next sample as soon as its current path ends (path
+// regeneration) instead of waiting for the warp's longest path; the warp
+// loops while any lane still has a path. The per-pixel sums still add the
+// samples in sample order, so the result is unchanged.
 template <int kStackN>
 __device__ __forceinline__ void pt_pixel(const DevScene &s, const PtLaunch &L, bool active, uint32_t px,
                                          uint32_t py, uint32_t &segments) {
@@ -67,100 +70,111 @@ __device__ __forceinline__ void pt_pixel(const DevScene &s, const PtLaunch &L, b
     double ax = 0, ay = 0, az = 0;
     if (active && L.sum64) ax = L.sum64[3 * pixel], ay = L.sum64[3 * pixel + 1], az = L.sum64[3 * pixel + 2];
     const bool any_geometry = s.n_refs > 0;
-    for (uint32_t smp = 0; smp < L.num_samples; smp++) {
-        pray_pcg32 rng = pray_pcg32_stream(L.seed, pixel, L.sample_offset + smp);
-        RayF r = prim;
-        float lr = 0.f, lg = 0.f, lb = 0.f;
-        float tr = 1.f, tg = 1.f, tb = 1.f;
-        uint32_t depth = 0;
-        bool alive = active;
-        while (__any_sync(kFull, alive)) {
-            float t;
-            const int pos = traverse<false, false, kStackN>(s, r, L.eps, 0.f, alive && any_geometry, t);
-            // next-event occlusion job of this bounce (mode 1)
-            bool need = false;
-            RayF sray = r;
-            float sd2 = 0.f, cxr = 0.f, cxg = 0.f, cxb = 0.f;
-            float4 nrm = make_float4(0.f, 0.f, 0.f, 0.f), col = nrm;
-            float hx = 0.f, hy = 0.f, hz = 0.f;
-            if (alive) {
-                segments++;
-                if (pos < 0) {
-                    if (L.mode == 0) lr = L.bg[0], lg = L.bg[1], lb = L.bg[2];
-                    else lr = lr + tr * L.bg[0], lg = lg + tg * L.bg[1], lb = lb + tb * L.bg[2];
+    // the lane's current path
+    uint32_t smp = 0;
+    pray_pcg32 rng;
+    RayF r = prim;
+    float lr = 0.f, lg = 0.f, lb = 0.f;
+    float tr = 1.f, tg = 1.f, tb = 1.f;
+    uint32_t depth = 0;
+    bool alive = false;
+    auto start = [&]() {
+        rng = pray_pcg32_stream(L.seed, pixel, L.sample_offset + smp);
+        r = prim;
+        lr = lg = lb = 0.f;
+        tr = tg = tb = 1.f;
+        depth = 0;
+        alive = true;
+    };
+    if (active && L.num_samples > 0) start();
+    while (__any_sync(kFull, alive)) {
+        const bool was_alive = alive;
+        float t;
+        const int pos = traverse<false, false, kStackN>(s, r, L.eps, 0.f, alive && any_geometry, t);
+        // next-event occlusion job of this bounce (mode 1)
+        bool need = false;
+        RayF sray = r;
+        float sd2 = 0.f, cxr = 0.f, cxg = 0.f, cxb = 0.f;
+        float4 nrm = make_float4(0.f, 0.f, 0.f, 0.f), col = nrm;
+        float hx = 0.f, hy = 0.f, hz = 0.f;
+        if (alive) {
+            segments++;
+            if (pos < 0) {
+                if (L.mode == 0) lr = L.bg[0], lg = L.bg[1], lb = L.bg[2];
+                else lr = lr + tr * L.bg[0], lg = lg + tg * L.bg[1], lb = lb + tb * L.bg[2];
+                alive = false;
+            } else {
+                const int id = (int)__float_as_uint(__ldg(&s.tris[pos].v0[3]));
+                nrm = shade_n(s, id), col = shade_c(s, id);
+                if (nrm.w != 0.f) {
+                    if (L.mode == 0) lr = col.x, lg = col.y, lb = col.z;
+                    else if (depth == 0) lr = lr + tr * col.x, lg = lg + tg * col.y, lb = lb + tb * col.z;
+                    alive = false;
+                } else if (depth >= L.max_depth) {
+                    if (L.mode == 0) lr = 0.f, lg = 0.f, lb = 0.f;
                     alive = false;
                 } else {
-                    const int id = (int)__float_as_uint(__ldg(&s.tris[pos].v0[3]));
-                    nrm = shade_n(s, id), col = shade_c(s, id);
-                    if (nrm.w != 0.f) {
-                        if (L.mode == 0) lr = col.x, lg = col.y, lb = col.z;
-                        else if (depth == 0) lr = lr + tr * col.x, lg = lg + tg * col.y, lb = lb + tb * col.z;
-                        alive = false;
-                    } else if (depth >= L.max_depth) {
-                        if (L.mode == 0) lr = 0.f, lg = 0.f, lb = 0.f;
-                        alive = false;
-                    } else {
-                        hx = r.ox + r.dx * t, hy = r.oy + r.dy * t, hz = r.oz + r.dz * t;
-                        if (L.mode != 0 && s.n_emit > 0) {
-                            const float ue = pray_uniform(&rng), ua = pray_uniform(&rng), ub = pray_uniform(&rng);
-                            const GTri *E = s.emit_tris + pick_emitter(s, ue);
-                            const float4 ev0 = __ldg(reinterpret_cast<const float4 *>(E->v0));
-                            const float4 ee1 = __ldg(reinterpret_cast<const float4 *>(E->e1));
-                            const float4 ee2 = __ldg(reinterpret_cast<const float4 *>(E->e2));
-                            const float su = sqrtf(ua);
-                            const float b1 = su * (1.f - ub), b2 = su * ub;
-                            const float yx = ev0.x + ee1.x * b1 + ee2.x * b2;
-                            const float yy = ev0.y + ee1.y * b1 + ee2.y * b2;
-                            const float yz = ev0.z + ee1.z * b1 + ee2.z * b2;
-                            float wx = yx - hx, wy = yy - hy, wz = yz - hz;
-                            const float d2 = wx * wx + wy * wy + wz * wz;
-                            if (d2 > 0.f) {
-                                const float inv = 1.0f / sqrtf(d2);
-                                wx *= inv, wy *= inv, wz *= inv;
-                                const int eid = (int)__float_as_uint(ev0.w);
-                                const float4 en = shade_n(s, eid), ec = shade_c(s, eid);
-                                const float cx = nrm.x * wx + nrm.y * wy + nrm.z * wz;
-                                const float cy = -(en.x * wx + en.y * wy + en.z * wz);
-                                if (cx > 0.f && cy > 0.f) {
-                                    need = true;
-                                    sray = make_ray(hx, hy, hz, wx, wy, wz);
-                                    sd2 = d2 * kShadowShrink;
-                                    const float g = ((cx * cy) * s.emit_area) * kInvPi / d2;
-                                    cxr = ((tr * col.x) * ec.x) * g;
-                                    cxg = ((tg * col.y) * ec.y) * g;
-                                    cxb = ((tb * col.z) * ec.z) * g;
-                                }
+                    hx = r.ox + r.dx * t, hy = r.oy + r.dy * t, hz = r.oz + r.dz * t;
+                    if (L.mode != 0 && s.n_emit > 0) {
+                        const float ue = pray_uniform(&rng), ua = pray_uniform(&rng), ub = pray_uniform(&rng);
+                        const GTri *E = s.emit_tris + pick_emitter(s, ue);
+                        const float4 ev0 = __ldg(reinterpret_cast<const float4 *>(E->v0));
+                        const float4 ee1 = __ldg(reinterpret_cast<const float4 *>(E->e1));
+                        const float4 ee2 = __ldg(reinterpret_cast<const float4 *>(E->e2));
+                        const float su = sqrtf(ua);
+                        const float b1 = su * (1.f - ub), b2 = su * ub;
+                        const float yx = ev0.x + ee1.x * b1 + ee2.x * b2;
+                        const float yy = ev0.y + ee1.y * b1 + ee2.y * b2;
+                        const float yz = ev0.z + ee1.z * b1 + ee2.z * b2;
+                        float wx = yx - hx, wy = yy - hy, wz = yz - hz;
+                        const float d2 = wx * wx + wy * wy + wz * wz;
+                        if (d2 > 0.f) {
+                            const float inv = 1.0f / sqrtf(d2);
+                            wx *= inv, wy *= inv, wz *= inv;
+                            const int eid = (int)__float_as_uint(ev0.w);
+                            const float4 en = shade_n(s, eid), ec = shade_c(s, eid);
+                            const float cx = nrm.x * wx + nrm.y * wy + nrm.z * wz;
+                            const float cy = -(en.x * wx + en.y * wy + en.z * wz);
+                            if (cx > 0.f && cy > 0.f) {
+                                need = true;
+                                sray = make_ray(hx, hy, hz, wx, wy, wz);
+                                sd2 = d2 * kShadowShrink;
+                                const float g = ((cx * cy) * s.emit_area) * kInvPi / d2;
+                                cxr = ((tr * col.x) * ec.x) * g;
+                                cxg = ((tg * col.y) * ec.y) * g;
+                                cxb = ((tb * col.z) * ec.z) * g;
                             }
                         }
                     }
                 }
             }
-            float dummy;
-            const bool occluded = traverse<true, false, kStackN>(s, sray, L.eps, sd2, need, dummy) >= 0;
-            if (need) {
-                segments++;
-                if (!occluded) lr = lr + cxr, lg = lg + cxg, lb = lb + cxb;
-            }
-            if (alive) {
-                // cosine bounce (and, in mode 1, Russian roulette)
-                if (L.mode == 0) alb_r[depth] = col.x, alb_g[depth] = col.y, alb_b[depth] = col.z;
-                const float u1 = pray_uniform(&rng), u2 = pray_uniform(&rng);
-                const float n3[3] = {nrm.x, nrm.y, nrm.z};
-                float d[3];
-                pray_sample_hemisphere(n3, u1, u2, d);
-                r = make_ray(hx, hy, hz, d[0], d[1], d[2]);
-                if (L.mode != 0) {
-                    tr = tr * col.x, tg = tg * col.y, tb = tb * col.z;
-                    if (depth >= L.rr_depth) {
-                        const float q = smin(smax(smax(tr, tg), tb), 0.95f);
-                        if (!(pray_uniform(&rng) < q)) alive = false;
-                        else tr = tr / q, tg = tg / q, tb = tb / q;
-                    }
-                }
-                depth++;
-            }
         }
-        if (active) {
+        float dummy;
+        const bool occluded = traverse<true, false, kStackN>(s, sray, L.eps, sd2, need, dummy) >= 0;
+        if (need) {
+            segments++;
+            if (!occluded) lr = lr + cxr, lg = lg + cxg, lb = lb + cxb;
+        }
+        if (alive) {
+            // cosine bounce (and, in mode 1, Russian roulette)
+            if (L.mode == 0) alb_r[depth] = col.x, alb_g[depth] = col.y, alb_b[depth] = col.z;
+            const float u1 = pray_uniform(&rng), u2 = pray_uniform(&rng);
+            const float n3[3] = {nrm.x, nrm.y, nrm.z};
+            float d[3];
+            pray_sample_hemisphere(n3, u1, u2, d);
+            r = make_ray(hx, hy, hz, d[0], d[1], d[2]);
+            if (L.mode != 0) {
+                tr = tr * col.x, tg = tg * col.y, tb = tb * col.z;
+                if (depth >= L.rr_depth) {
+                    const float q = smin(smax(smax(tr, tg), tb), 0.95f);
+                    if (!(pray_uniform(&rng) < q)) alive = false;
+                    else tr = tr / q, tg = tg / q, tb = tb / q;
+                }
+            }
+            depth++;
+        }
+        if (was_alive && !alive) {
+            // the path ended: its value joins the pixel's sums in sample order
             if (L.mode == 0) {
                 while (depth > 0) {
                     depth--;
@@ -169,6 +183,7 @@ __device__ __forceinline__ void pt_pixel(const DevScene &s, const PtLaunch &L, b
             }
             sr = sr + lr, sg = sg + lg, sb = sb + lb;
             if (L.sum64) ax = ax + (double)lr, ay = ay + (double)lg, az = az + (double)lb;
+            if (++smp < L.num_samples) start();
         }
     }
     if (active) {
