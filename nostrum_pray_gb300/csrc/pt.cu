@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(128) k_render_pt_diffuse(DevScene s, PtLaunch 
 }  // namespace
 
 cudaError_t launch_render_pt(const DevScene &s, const PtLaunch &L, cudaStream_t stream) {
-    const uint64_t tiles = (uint64_t)((L.cam.width + 7) / 8) * ((L.cam.height + 3) / 4);
+    const uint64_t tiles = warp_tiles(L.cam.width, L.cam.height);
     const uint64_t threads = tiles * 32;
     if (threads == 0) return cudaSuccess;
     const unsigned bs = 128;

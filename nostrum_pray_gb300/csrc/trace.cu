@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(128) k_features(DevScene s, CameraConsts cam, 
 }  // namespace
 
 cudaError_t launch_features(const DevScene &s, const CameraConsts &cam, float eps, __half *out, cudaStream_t stream) {
-    const uint64_t threads = (uint64_t)((cam.width + 7) / 8) * ((cam.height + 3) / 4) * 32;
+    const uint64_t threads = warp_tiles(cam.width, cam.height) * 32;
     k_features<<<(unsigned)((threads + 127) / 128), 128, 0, stream>>>(s, cam, eps, out);
     return cudaGetLastError();
 }
@@ -171,7 +171,7 @@ cudaError_t launch_trace_closest(const DevScene &s, const float *rays, uint64_t 
 }
 
 cudaError_t launch_render_rt(const DevScene &s, const RtLaunch &L, cudaStream_t stream) {
-    const uint64_t tiles = (uint64_t)((L.cam.width + 7) / 8) * ((L.cam.height + 3) / 4);
+    const uint64_t tiles = warp_tiles(L.cam.width, L.cam.height);
     const uint64_t threads = tiles * 32;
     if (threads == 0) return cudaSuccess;
     const unsigned bs = 128, grid = (unsigned)((threads + bs - 1) / bs);

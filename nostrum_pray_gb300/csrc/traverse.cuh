@@ -303,13 +303,21 @@ __device__ __forceinline__ RayF primary_ray(const CameraConsts &c, uint32_t px, 
 // int, keep the low byte.
 __device__ __forceinline__ uint32_t quantise(float v) { return (uint32_t)(int32_t)(v * 255.f + 0.5f) & 0xFFu; }
 
-// Pixel index of thread i: warps cover 8x4 pixel tiles, tiles row-major.
+// Pixel index of thread i: warps cover kWarpTileW x kWarpTileH pixel tiles,
+// tiles row-major.
+constexpr uint32_t kWarpTileW = 8, kWarpTileH = 4;
+static_assert(kWarpTileW * kWarpTileH == 32, "a warp tile holds 32 pixels");
+
+__host__ __device__ __forceinline__ uint64_t warp_tiles(uint32_t w, uint32_t h) {
+    return (uint64_t)((w + kWarpTileW - 1) / kWarpTileW) * ((h + kWarpTileH - 1) / kWarpTileH);
+}
+
 __device__ __forceinline__ bool pixel_of(uint64_t i, uint32_t w, uint32_t h, uint32_t &px, uint32_t &py) {
-    const uint32_t tiles_x = (w + 7) / 8;
+    const uint32_t tiles_x = (w + kWarpTileW - 1) / kWarpTileW;
     const uint64_t tile = i >> 5;
     const uint32_t lane = (uint32_t)i & 31u;
-    px = (uint32_t)(tile % tiles_x) * 8 + (lane & 7u);
-    py = (uint32_t)(tile / tiles_x) * 4 + (lane >> 3);
+    px = (uint32_t)(tile % tiles_x) * kWarpTileW + lane % kWarpTileW;
+    py = (uint32_t)(tile / tiles_x) * kWarpTileH + lane / kWarpTileW;
     return px < w && py < h;
 }
 
