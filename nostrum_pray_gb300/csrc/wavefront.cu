@@ -42,6 +42,7 @@ constexpr float kInvPi = 0.318309886183790671538f;
 constexpr float kShadowShrink = 0.999f;
 constexpr int kThreads = 256;
 constexpr int kRefillIdle = 8;  // dynamic fetch: refill a warp's idle lanes once this many are idle
+constexpr int kTraceBlocksPerSm = 4;  // resident blocks per SM of the extend and occlusion passes (register cap)
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
@@ -117,7 +118,8 @@ __device__ __forceinline__ uint32_t warp_fetch(uint32_t *counter, unsigned idle,
 // (reset by the shade pass); counts[4], the occlusion pass's counter, is
 // reset here.
 template <int kStackN>
-__global__ void __launch_bounds__(kThreads) k_wf_extend(DevScene s, PtLaunch L, WavefrontScratch w, int in, int out) {
+__global__ void __launch_bounds__(kThreads, kTraceBlocksPerSm) k_wf_extend(DevScene s, PtLaunch L, WavefrontScratch w,
+                                                                         int in, int out) {
     constexpr unsigned kFull = 0xFFFFFFFFu;
     const uint32_t n = w.counts[in];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -262,7 +264,8 @@ __global__ void __launch_bounds__(kThreads) k_wf_shade(DevScene s, PtLaunch L, W
 // Any-hit test of every occlusion job, with the same dynamic fetch
 // (counts[4]); an unoccluded job adds its contribution to its path.
 template <int kStackN>
-__global__ void __launch_bounds__(kThreads) k_wf_occlude(DevScene s, PtLaunch L, WavefrontScratch w) {
+__global__ void __launch_bounds__(kThreads, kTraceBlocksPerSm) k_wf_occlude(DevScene s, PtLaunch L,
+                                                                          WavefrontScratch w) {
     constexpr unsigned kFull = 0xFFFFFFFFu;
     const uint32_t n = w.counts[2];
     uint32_t seg = 0;
@@ -394,7 +397,7 @@ cudaError_t record_wavefront_frame(const DevScene &s, const PtLaunch &L, const W
     const uint64_t P = (uint64_t)L.cam.width * L.cam.height;
     if (P == 0 || L.num_samples == 0) return cudaSuccess;
     const uint32_t S = (uint32_t)std::min<uint64_t>(L.num_samples, std::max<uint64_t>(1, w.capacity / P));
-    const unsigned grid = (unsigned)std::max(1, sm_count) * 4;
+    const unsigned grid = (unsigned)std::max(1, sm_count) * kTraceBlocksPerSm;
     const bool small_stack = s.depth < 32;  // a 32-entry traversal stack suffices
     for (uint32_t base = 0; base < L.num_samples; base += S) {
         const uint32_t Sr = std::min(S, L.num_samples - base);
