@@ -42,7 +42,7 @@ constexpr float kInvPi = 0.318309886183790671538f;
 constexpr float kShadowShrink = 0.999f;
 constexpr int kThreads = 256;
 constexpr int kRefillIdle = 8;  // dynamic fetch: refill a warp's idle lanes once this many are idle
-constexpr int kTraceBlocksPerSm = 4;  // resident blocks per SM of the extend and occlusion passes (register cap)
+constexpr int kTraceBlocksPerSm = 5;  // resident blocks per SM of the extend and occlusion passes (register cap)
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
