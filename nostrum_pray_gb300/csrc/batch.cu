@@ -26,7 +26,7 @@ namespace {
 using namespace dev;
 
 template <int kStackN>
-__global__ void k_batch_pt(BatchLaunch B) {
+__global__ void __launch_bounds__(256, 4) k_batch_pt(BatchLaunch B) {
     constexpr unsigned kFull = 0xFFFFFFFFu;
     const uint32_t lane = threadIdx.x & 31u;
     while (true) {

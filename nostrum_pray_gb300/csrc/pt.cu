@@ -14,7 +14,7 @@ namespace {
 
 using namespace dev;
 
-__global__ void __launch_bounds__(128) k_render_pt(DevScene s, PtLaunch L) {
+__global__ void __launch_bounds__(128, 10) k_render_pt(DevScene s, PtLaunch L) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t px, py;
     const bool active = pixel_of(i, L.cam.width, L.cam.height, px, py);
