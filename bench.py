@@ -235,7 +235,7 @@ def run_ours(args):
     else:
         torch.cuda.set_device(0)
     dev = torch.cuda.current_device()
-    from nostrum_pray_gb300 import native
+    from nostrum_pray_gb300 import native, replicas
     try:
         native.lib()
     except native.PrayError:
@@ -258,8 +258,7 @@ def run_ours(args):
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     sampler = ClockSampler(dev) if rank == 0 else None
-    if world > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     torch.cuda.synchronize()
     if sampler:
         sampler.start()
@@ -271,17 +270,13 @@ def run_ours(args):
         sc.render_rt(setup, rgb, stream=stream)
         ends[k].record(stream)
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     wall = time.perf_counter() - wall0
     clocks = sampler.stop() if sampler else None
     times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     kernel_ms = sum(times)
-    t_local = torch.tensor([kernel_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t_local, op=torch.distributed.ReduceOp.MAX)
-    kernel_ms_max = float(t_local.item())
-    value = rays_per_frame * args.steps * world / (kernel_ms_max / 1e3) / 1e6
+    kernel_ms_max = replicas.slowest(kernel_ms, "cuda")
+    value = replicas.whole_job_rate(rays_per_frame * args.steps, kernel_ms / 1e3, "cuda") / 1e6
 
     # end to end through the host-memory C ABI entry point (params in, image out)
     for _ in range(2):
@@ -291,7 +286,7 @@ def run_ours(args):
         t0 = time.perf_counter()
         img, _ = sc.render_rt_host(setup)
         e2e_times.append(time.perf_counter() - t0)
-    e2e_val = rays_per_frame * world / statistics.mean(e2e_times) / 1e6
+    e2e_val = replicas.whole_job_rate(rays_per_frame, statistics.mean(e2e_times), "cuda") / 1e6
 
     # roofline of the render kernel: algorithmic bytes per launch
     prim, occl, pairs, tris, hits = (int(x) for x in counts)
