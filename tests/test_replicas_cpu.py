@@ -32,7 +32,7 @@ def _rank(rank, world, port, out):
 
 def test_two_gloo_ranks_time_like_the_bench():
     world = 2
-    manager = mp.Manager()
+    manager = mp.get_context("spawn").Manager()
     out = manager.dict()
     mp.spawn(_rank, args=(world, _free_port(), out), nprocs=world, join=True)
     for r in range(world):
