@@ -85,8 +85,11 @@ typedef enum {
 
 typedef enum {
     PRAY_SCHED_PIXEL = 0,      /* one thread per pixel, samples and bounces in a loop */
-    PRAY_SCHED_WAVEFRONT = 1   /* path pool + extend / shade / occlusion passes with compacted queues,
+    PRAY_SCHED_WAVEFRONT = 1,  /* path pool + extend / shade / occlusion passes with compacted queues,
                                   one CUDA graph per frame; PRAY_PT_NEE only */
+    PRAY_SCHED_AUTO = 2        /* PRAY_SCHED_WAVEFRONT for PRAY_PT_NEE frames of at least 2^19 paths
+                                  (width x height x num_samples), PRAY_SCHED_PIXEL otherwise; both give
+                                  the same result */
 } pray_pt_scheduler;
 
 typedef struct {

@@ -207,8 +207,9 @@ pray_status check_pt_params(const pray_pt_params *p) {
         return set_error(PRAY_ERR_INVALID_ARGUMENT, "mode must be PRAY_PT_KAJIYA, PRAY_PT_NEE or PRAY_PT_DIFFUSE");
     if (p->mode == PRAY_PT_DIFFUSE && p->max_depth > (uint32_t)kMaxDiffuseDepth)
         return set_error(PRAY_ERR_UNSUPPORTED, "PRAY_PT_DIFFUSE: max_depth must be at most 8");
-    if (p->scheduler != PRAY_SCHED_PIXEL && p->scheduler != PRAY_SCHED_WAVEFRONT)
-        return set_error(PRAY_ERR_INVALID_ARGUMENT, "scheduler must be PRAY_SCHED_PIXEL or PRAY_SCHED_WAVEFRONT");
+    if (p->scheduler != PRAY_SCHED_PIXEL && p->scheduler != PRAY_SCHED_WAVEFRONT && p->scheduler != PRAY_SCHED_AUTO)
+        return set_error(PRAY_ERR_INVALID_ARGUMENT,
+                         "scheduler must be PRAY_SCHED_PIXEL, PRAY_SCHED_WAVEFRONT or PRAY_SCHED_AUTO");
     if (p->scheduler == PRAY_SCHED_WAVEFRONT && p->mode != PRAY_PT_NEE)
         return set_error(PRAY_ERR_UNSUPPORTED, "the wavefront scheduler runs PRAY_PT_NEE only");
     if ((uint64_t)p->sample_offset + p->num_samples > 0xFFFFFFFFull)
@@ -265,9 +266,19 @@ pray_status ensure_frame(pray_scene *s, uint64_t bytes) {
 // Most paths a wavefront round keeps in flight (at least one per pixel).
 constexpr uint64_t kWavefrontMaxPaths = 1ull << 23;
 
+// Paths per frame from which PRAY_SCHED_AUTO picks the wavefront scheduler:
+// below it the per-pixel kernel is faster (one launch instead of three per
+// bounce; at 512 x 512 it wins at 1 sample per pixel and loses at 2).
+constexpr uint64_t kAutoWavefrontPaths = 1ull << 19;
+
 // Runs a path-tracing launch with the chosen scheduler on `stream`.
 pray_status run_pt(pray_scene *s, const PtLaunch &L, int scheduler, uint32_t wavefront_paths, cudaStream_t stream) {
     cudaError_t e;
+    if (scheduler == PRAY_SCHED_AUTO)
+        scheduler = (L.mode == PRAY_PT_NEE &&
+                     (uint64_t)L.cam.width * L.cam.height * L.num_samples >= kAutoWavefrontPaths)
+                        ? PRAY_SCHED_WAVEFRONT
+                        : PRAY_SCHED_PIXEL;
     if (scheduler == PRAY_SCHED_PIXEL) {
         e = launch_render_pt(s->view(), L, stream);
         return e == cudaSuccess ? PRAY_OK : cuda_error(e, "render_pt launch");

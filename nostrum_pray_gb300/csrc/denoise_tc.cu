@@ -63,7 +63,7 @@ struct TcArgs {
     int taps_per_split, taps_per_stage, stages;
     int tmem_cols;
     uint32_t w_off, bar_off;  // shared-memory offsets (the halo is at 0)
-    uint32_t halo_stride;     // persistent kernel: offset of the second halo buffer
+    uint32_t halo_stride;     // persistent kernel: distance between the halo ring's slots
     int *err;
 };
 
@@ -137,19 +137,20 @@ __device__ __forceinline__ uint32_t pack2(float a, float b) {
     return *reinterpret_cast<const uint32_t *>(&v);
 }
 
-// Epilogue of one tile: warp w reads TMEM lanes 32w..32w+31 (tile rows m =
-// pixel (m / 8, m % 8)) from column `tmem` on, 16 columns at a time, and
-// stores bias + ReLU + BF16 (16-byte stores), FP32, or raw FP32 partials.
-__device__ __forceinline__ void epilogue(const TcArgs &P, uint32_t tmem, int img, int y0, int x0, int split) {
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const int m = warp * 32 + (tid & 31);
+// Epilogue of one tile: the calling warp reads TMEM lanes 32q..32q+31 (q =
+// quad, the warp's lane quadrant: its warp index mod 4; tile rows m = pixel
+// (m / 8, m % 8)) from column `tmem` on, 16 columns at a time, and stores
+// bias + ReLU + BF16 (16-byte stores), FP32, or raw FP32 partials.
+__device__ __forceinline__ void epilogue(const TcArgs &P, uint32_t tmem, int img, int y0, int x0, int split,
+                                         int quad) {
+    const int m = quad * 32 + (int)(threadIdx.x & 31);
     const int yy = y0 + (m >> 3), xx = x0 + (m & 7);
     const bool valid = yy < P.h && xx < P.wd;
     const size_t M = (size_t)P.n * P.h * P.wd;
     const size_t pix = ((size_t)img * P.h + yy) * P.wd + xx;
     for (int c0 = 0; c0 < P.npad; c0 += 16) {
         uint32_t r[16];
-        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+        const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0;
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
             "[%16];"
@@ -290,7 +291,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtenso
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     __syncthreads();
     if (!ok && tid == 0) atomicExch(P.err, 1);
-    if (ok) epilogue(P, tmem, img, y0, x0, split);
+    if (ok) epilogue(P, tmem, img, y0, x0, split, warp);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) {
@@ -300,27 +301,48 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtenso
     }
 }
 
-// Persistent, pipelined variant for levels that need no tap split and whose
-// weights fit in shared memory next to two halos: each CTA loads the
-// weights once, then walks tiles blockIdx.x, blockIdx.x + gridDim.x, ...
-// with two halo buffers and two TMEM accumulators, so that the halo of tile
-// i + 1 is in flight and the MMAs of tile i run while the epilogue of tile
-// i - 1 drains.
-//   iteration i: thread 0 waits for halo i, issues its MMAs into
-//   accumulator i % 2 and commits them; then (i >= 1) every thread waits for
-//   the MMAs of tile i - 1, thread 0 starts the halo load of tile i + 1 into
-//   the buffer tile i - 1 used, and all warps run the epilogue of tile i - 1.
-__global__ void __launch_bounds__(128) k_conv_tc_persistent(const __grid_constant__ CUtensorMap xmap, TcArgs P) {
+__device__ __forceinline__ void mbar_init_count(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+constexpr int kWsThreads = 192;  // warp 0 loads, warp 1 issues MMAs, warps 2-5 drain accumulators
+
+// Persistent, warp-specialised variant for levels that need no tap split and
+// whose weights fit in shared memory beside a ring of halos. Each CTA loads
+// the weights once and walks tiles blockIdx.x, blockIdx.x + gridDim.x, ...:
+//   warp 0 (one thread) loads tile i's halo into ring slot i % H once the
+//     MMAs of tile i - H have released it;
+//   warp 1 (one thread) waits for the halo and for accumulator i % 2 to be
+//     drained, issues the tile's MMAs into it and commits them to the slot's
+//     "released" and the accumulator's "full" barriers;
+//   warps 2-5 (one TMEM lane quadrant each) drain accumulator i % 2 to
+//     global memory and release it.
+// So halo loads, MMAs and epilogues of consecutive tiles overlap. Every wait
+// is bounded; a timeout sets a shared abort flag that ends every role's
+// loop, and the copies and MMAs in flight are waited for (bounded) before
+// the shared memory and TMEM are released.
+__global__ void __launch_bounds__(kWsThreads) k_conv_tc_persistent(const __grid_constant__ CUtensorMap xmap,
+                                                                   TcArgs P) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int H = P.stages;  // halo ring slots
     const int nchunk = P.cin >> 3;
     const uint32_t halo0 = smem_u32(smem), wbase = halo0 + P.w_off;
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + P.bar_off);
-    // bars[0..1] halo b loaded, bars[2..3] MMAs of accumulator b done,
-    // bars[4] weights loaded, bars[5] final drain
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 6);
-    int *fail = reinterpret_cast<int *>(tmem_slot + 1);
+    // bars: [0, H) halo loaded, [H, 2H) halo released, 2H + a accumulator
+    // full, 2H + 2 + a accumulator drained, 2H + 4 weights loaded, 2H + 5
+    // final drain of the MMAs
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * H + 6);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    volatile int *issued = reinterpret_cast<volatile int *>(tmem_slot + 2);    // halos loaded so far
+    volatile int *consumed = reinterpret_cast<volatile int *>(tmem_slot + 3);  // halos the MMA warp waited for
+    volatile int *w_waited = reinterpret_cast<volatile int *>(tmem_slot + 4);
     auto bar = [&](int i) { return smem_u32(&bars[i]); };
+    const int full0 = 0, empty0 = H, accf0 = 2 * H, acce0 = 2 * H + 2, wbar = 2 * H + 4, dbar = 2 * H + 5;
     const int per_img = P.tiles_x * P.tiles_y;
     const int tiles = P.n * per_img;
     const int items = tiles > (int)blockIdx.x ? (tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
@@ -341,46 +363,57 @@ __global__ void __launch_bounds__(128) k_conv_tc_persistent(const __grid_constan
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        for (int i = 0; i < 6; i++) mbar_init(bar(i));
-        *fail = 0;
+        for (int i = 0; i < 2 * H; i++) mbar_init(bar(i));
+        mbar_init(bar(accf0)), mbar_init(bar(accf0 + 1));
+        mbar_init_count(bar(acce0), 128), mbar_init_count(bar(acce0 + 1), 128);
+        mbar_init(bar(wbar)), mbar_init(bar(dbar));
+        *abort_flag = 0, *issued = 0, *consumed = 0, *w_waited = 0;
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-    const uint32_t idesc = inst_desc(128, P.npad);
 
-    // thread 0's bookkeeping of copies issued and waited for (drained on exit)
-    int halos_issued = 0, halos_waited = 0;
-    bool w_waited = false;
-    auto load_halo = [&](int i) {
-        int img, y0, x0;
-        tile_of(i, img, y0, x0);
-        const int b = i & 1;
-        const uint32_t dst = halo0 + b * P.halo_stride;
-        mbar_expect_tx(bar(b), (uint32_t)nchunk * kChunkBytes);
-        for (int c = 0; c < nchunk; c++) tma_halo(dst + c * kPlaneBytes, &xmap, bar(b), 8 * c, x0 - 1, y0 - 1, img);
-        halos_issued = i + 1;
-    };
-    if (tid == 0 && items > 0) {
-        mbar_expect_tx(bar(4), wbytes);
-        bulk_copy(wbase, P.w, wbytes, bar(4));
-        load_halo(0);
-        if (items > 1) load_halo(1);
-        if (!mbar_wait(bar(4), 0)) *fail = 1;
-        w_waited = true;
-    }
-    __syncthreads();
-    int done = 0;  // tiles whose epilogue ran
-    for (int i = 0; i < items && !*fail; i++) {
-        const int b = i & 1;
-        if (tid == 0) {
-            if (mbar_wait(bar(b), (uint32_t)(i >> 1) & 1)) {
-                halos_waited = i + 1;
+    if (warp == 0) {
+        if (lane == 0 && items > 0) {
+            mbar_expect_tx(bar(wbar), wbytes);
+            bulk_copy(wbase, P.w, wbytes, bar(wbar));
+            for (int i = 0; i < items && !*abort_flag; i++) {
+                const int h = i % H;
+                if (i >= H && !mbar_wait(bar(empty0 + h), (uint32_t)((i / H) - 1) & 1)) {
+                    *abort_flag = 1;
+                    break;
+                }
+                int img, y0, x0;
+                tile_of(i, img, y0, x0);
+                const uint32_t dst = halo0 + (uint32_t)h * P.halo_stride;
+                mbar_expect_tx(bar(full0 + h), (uint32_t)nchunk * kChunkBytes);
+                for (int c = 0; c < nchunk; c++)
+                    tma_halo(dst + c * kPlaneBytes, &xmap, bar(full0 + h), 8 * c, x0 - 1, y0 - 1, img);
+                *issued = i + 1;
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0 && items > 0) {
+            bool ok = mbar_wait(bar(wbar), 0);
+            *w_waited = 1;
+            if (!ok) *abort_flag = 1;
+            const uint32_t idesc = inst_desc(128, P.npad);
+            for (int i = 0; i < items && ok && !*abort_flag; i++) {
+                const int h = i % H, a = i & 1;
+                if (!mbar_wait(bar(full0 + h), (uint32_t)(i / H) & 1)) {
+                    *abort_flag = 1;
+                    break;
+                }
+                *consumed = i + 1;
+                if (i >= 2 && !mbar_wait(bar(acce0 + a), (uint32_t)((i >> 1) - 1) & 1)) {
+                    *abort_flag = 1;
+                    break;
+                }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t acc = tmem + (uint32_t)(b * acc_stride);
-                const uint32_t hb = halo0 + b * P.halo_stride;
+                const uint32_t acc = tmem + (uint32_t)(a * acc_stride);
+                const uint32_t hb = halo0 + (uint32_t)h * P.halo_stride;
                 for (int tap = 0; tap < 9; tap++) {
                     const int dy = tap / 3, dx = tap - 3 * (tap / 3);
                     const uint32_t a0 = hb + (uint32_t)(dy * kHaloW + dx) * 16;
@@ -391,54 +424,37 @@ __global__ void __launch_bounds__(128) k_conv_tc_persistent(const __grid_constan
                         mma(acc, ad, bd, idesc, (tap | p) != 0 ? 1u : 0u);
                     }
                 }
-            } else {
-                *fail = 1;
+                commit(bar(empty0 + h));
+                commit(bar(accf0 + a));
             }
-            commit(bar(2 + b));
+            // everything this thread issued completes before TMEM is freed
+            commit(bar(dbar));
+            mbar_wait(bar(dbar), 0);
         }
-        if (i >= 1) {
-            const int j = i - 1, bj = j & 1;
-            if (!mbar_wait(bar(2 + bj), (uint32_t)(j >> 1) & 1)) atomicExch(fail, 1);
-            // the MMAs of tile j are done: its halo buffer takes tile i + 1
-            if (tid == 0 && !*fail && i + 1 < items) load_halo(i + 1);
-        }
-        __syncthreads();
-        if (*fail) break;
-        if (i >= 1) {
-            const int j = i - 1;
-            int img, y0, x0;
-            tile_of(j, img, y0, x0);
+    } else {
+        const int quad = warp & 3;  // warps 2, 3, 4, 5 -> TMEM lane quadrants 2, 3, 0, 1
+        // every decision warp-uniform: the TMEM loads below are warp-collective
+        for (int i = 0; i < items; i++) {
+            if (__any_sync(0xFFFFFFFFu, *abort_flag != 0)) break;
+            const int a = i & 1;
+            if (!__all_sync(0xFFFFFFFFu, mbar_wait(bar(accf0 + a), (uint32_t)(i >> 1) & 1))) {
+                if (lane == 0) *abort_flag = 1;
+                break;
+            }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            epilogue(P, tmem + (uint32_t)((j & 1) * acc_stride), img, y0, x0, 0);
-            done = i;
+            int img, y0, x0;
+            tile_of(i, img, y0, x0);
+            epilogue(P, tmem + (uint32_t)(a * acc_stride), img, y0, x0, 0, quad);
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            __syncthreads();
+            mbar_arrive(bar(acce0 + a));
         }
     }
-    if (!*fail && items > 0) {
-        // the last tile
-        const int j = items - 1, bj = j & 1;
-        const bool ok = mbar_wait(bar(2 + bj), (uint32_t)(j >> 1) & 1);
-        if (!ok) atomicExch(fail, 1);
-        __syncthreads();
-        if (!*fail) {
-            int img, y0, x0;
-            tile_of(j, img, y0, x0);
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            epilogue(P, tmem + (uint32_t)(bj * acc_stride), img, y0, x0, 0);
-            done = items;
-        }
-    }
-    (void)done;
-    if (tid == 0) {
-        if (*fail) {
-            atomicExch(P.err, 1);
-            // drain what is still in flight (bounded) before the shared memory goes away
-            if (!w_waited && items > 0) mbar_wait(bar(4), 0);
-            for (int i = halos_waited; i < halos_issued; i++) mbar_wait(bar(i & 1), (uint32_t)(i >> 1) & 1);
-        }
-        commit(bar(5));
-        mbar_wait(bar(5), 0);
+    __syncthreads();
+    if (tid == 0 && *abort_flag) {
+        atomicExch(P.err, 1);
+        // copies still in flight (bounded) before the shared memory goes away
+        if (items > 0 && !*w_waited) mbar_wait(bar(wbar), 0);
+        for (int j = *consumed; j < *issued; j++) mbar_wait(bar(full0 + j % H), (uint32_t)(j / H) & 1);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -570,10 +586,13 @@ cudaError_t tc_conv_plan(TcConvPlan &p, const __nv_bfloat16 *x, int n, int h, in
     size_t smem;
     int cols = 32;
     if (p.persistent) {
+        // a ring of three halos when it fits, else two
+        const int ring = 3 * halo + 9 * wtap + 128 <= kSmemPersistent ? 3 : 2;
+        p.stages = ring;
         p.halo_stride = (uint32_t)halo;
-        p.w_off = (uint32_t)(2 * halo);
-        p.bar_off = (uint32_t)((2 * halo + 9 * wtap + 15) & ~(size_t)15);
-        smem = p.bar_off + 8 * 6 + 16;
+        p.w_off = (uint32_t)(ring * halo);
+        p.bar_off = (uint32_t)((ring * halo + 9 * wtap + 15) & ~(size_t)15);
+        smem = p.bar_off + 8 * (2 * (size_t)ring + 6) + 32;
         while (cols < 2 * ((p.npad + 31) & ~31)) cols <<= 1;
     } else {
         p.halo_stride = 0;
@@ -638,7 +657,7 @@ cudaError_t conv3x3_forward_tc(const TcConvPlan &p, const __nv_bfloat16 *wpacked
     CUtensorMap map;
     std::memcpy(&map, p.tmap, sizeof(map));
     if (p.persistent)
-        k_conv_tc_persistent<<<(unsigned)p.grid, 128, p.smem, st>>>(map, a);
+        k_conv_tc_persistent<<<(unsigned)p.grid, kWsThreads, p.smem, st>>>(map, a);
     else
         k_conv_tc<<<dim3((unsigned)p.tiles, (unsigned)p.splits), 128, p.smem, st>>>(map, a);
     cudaError_t e = cudaGetLastError();

@@ -71,7 +71,7 @@ def _setup(cfg: DenoiseConfig, res: Optional[int] = None):
 
 def _params(cfg, st, spp, seed, offset=0):
     return native.pt_params(st, spp=spp, max_depth=cfg.depth, seed=seed, mode=native.PT_NEE,
-                            rr_depth=cfg.rr_depth, scheduler=native.SCHED_WAVEFRONT, sample_offset=offset)
+                            rr_depth=cfg.rr_depth, scheduler=native.SCHED_AUTO, sample_offset=offset)
 
 
 def render_room(cfg: DenoiseConfig, room_seed: int, torch, res: Optional[int] = None):

@@ -25,7 +25,7 @@ CLI_PATH = os.path.join(_PKG, "_build", "Pray")
 PRAY_OK = 0
 TREE_MEDIAN, TREE_SAH = 0, 1
 PT_KAJIYA, PT_NEE, PT_DIFFUSE = 0, 1, 2
-SCHED_PIXEL, SCHED_WAVEFRONT = 0, 1
+SCHED_PIXEL, SCHED_WAVEFRONT, SCHED_AUTO = 0, 1, 2
 
 _vp = ctypes.c_void_p
 _u64 = ctypes.c_uint64

@@ -171,3 +171,24 @@ def test_diffuse_mode_limits():
     rgb = torch.empty((16, 16, 3), dtype=torch.uint8, device="cuda")
     with pytest.raises(native.PrayError):
         native.Batch([sc], [native.pt_params(st, spp=2, max_depth=1, mode=native.PT_DIFFUSE)], [(rgb, None)])
+
+
+def test_auto_scheduler_gives_the_same_frames():
+    """PRAY_SCHED_AUTO (per-pixel kernel below 2^19 paths, wavefront from
+    there on) returns the frames of the fixed schedulers, bit for bit."""
+    m = scenes.room(grid=6)
+    for (w, h, spp) in ((64, 64, 4), (128, 128, 32)):
+        st = scenes.room_setup(w, h)
+        sc = native.Scene.from_setup(m, st)
+        got = {}
+        for sched in (native.SCHED_PIXEL, native.SCHED_WAVEFRONT, native.SCHED_AUTO):
+            p = native.pt_params(st, spp=spp, max_depth=8, seed=21, mode=native.PT_NEE, rr_depth=3, scheduler=sched)
+            got[sched] = sc.render_pt_host(p)[1]
+        np.testing.assert_array_equal(got[native.SCHED_AUTO], got[native.SCHED_PIXEL])
+        np.testing.assert_array_equal(got[native.SCHED_AUTO], got[native.SCHED_WAVEFRONT])
+    # Kajiya frames always run per pixel under AUTO
+    st = scenes.room_setup(128, 128)
+    sc = native.Scene.from_setup(m, st)
+    a = sc.render_pt_host(native.pt_params(st, spp=32, max_depth=4, seed=2, scheduler=native.SCHED_AUTO))[1]
+    b = sc.render_pt_host(native.pt_params(st, spp=32, max_depth=4, seed=2, scheduler=native.SCHED_PIXEL))[1]
+    np.testing.assert_array_equal(a, b)
