@@ -4,9 +4,10 @@ Workload (default): the 1.31M-triangle displaced icosphere (20 faces
 subdivided 8 times, radius 1, radial value-noise displacement 0.05), SAH kd
 tree (traversal cost 1, intersection cost 1.5), 1920x1080, one primary ray per
 pixel plus one occlusion ray per light (2 point lights) where the light is in
-front of the surface. det threshold 0 (the reference's 1e-4 culls every
-triangle of this sphere). One step = one frame rendered by the
-fused ray-tracing kernel with the scene resident in HBM.
+front of the surface. det threshold 0 (the reference's absolute 1e-4 culls
+every triangle of this unit sphere, whose |ab x ac| are about 2e-5). One step =
+one frame rendered by the fused ray-tracing kernel with the scene resident in
+HBM.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
