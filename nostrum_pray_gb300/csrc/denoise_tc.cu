@@ -25,6 +25,7 @@
 // Every mbarrier wait is bounded: on timeout the kernel records an error,
 // stops issuing, waits (bounded) for the copies and MMAs it issued, and frees
 // its TMEM.
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 
@@ -635,13 +636,18 @@ cudaError_t tc_conv_plan(TcConvPlan &p, const __nv_bfloat16 *x, int n, int h, in
 cudaError_t conv3x3_forward_tc(const TcConvPlan &p, const __nv_bfloat16 *wpacked, const float *bias,
                                __nv_bfloat16 *y, float *y32, float *partial, int *err, cudaStream_t st) {
     if (p.splits > 1 && !partial) return cudaErrorInvalidValue;
-    static bool attr_set = false;
-    if (!attr_set) {
+    // the shared-memory opt-in is a per-device setting of each kernel: once per device
+    static std::atomic<uint64_t> attr_set{0};
+    int dev = 0;
+    cudaError_t e0 = cudaGetDevice(&dev);
+    if (e0 != cudaSuccess) return e0;
+    const uint64_t bit = dev < 64 ? 1ull << dev : 0;
+    if (!bit || !(attr_set.load() & bit)) {
         cudaError_t e = cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_conv_tc_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax);
         if (e != cudaSuccess) return e;
-        attr_set = true;
+        attr_set.fetch_or(bit);
     }
     TcArgs a;
     a.w = wpacked, a.bias = bias;
