@@ -371,13 +371,30 @@ def run_pt(args):
     paths, segs = int(cnt[0]), int(cnt[1])
     ms = _timed_frames(lambda: sc.render_pt(p, rgb), args.steps, args.warmup, flush)
     sec = ms / 1e3
+    cpu = None
+    if not args.no_cpu_baseline:
+        # the oracle's restatement of the same path tracer (full depth-first
+        # traversal per ray) on whole central rows, until the time budget
+        from oracle import oracle as O
+        O.build()
+        orc = O.OracleScene.from_setup(mesh, st)
+        thr = O.default_threads()
+        row, rows, elapsed = st.height // 2, 0, 0.0
+        while elapsed < args.cpu_seconds and row < st.height:
+            t0 = time.perf_counter()
+            orc.render_pt(st, spp=spp, max_depth=8, seed=1, mode=native.PT_NEE, rr_depth=3, rows=(row, row + 1),
+                          threads=thr)
+            elapsed += time.perf_counter() - t0
+            row, rows = row + 1, rows + 1
+        cpu = {"value": round(rows * st.width * spp / elapsed / 1e6, 5), "unit": "Msamples/s", "cores": thr,
+               "kind": "port", "sample": f"{rows} central rows of {st.height} at {spp} spp in {elapsed:.1f} s"}
     line = {"metric": "Msamples/s", "value": round(paths * args.steps / sec / 1e6, 2), "unit": "Msamples/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"closed room {mesh.n} triangles, 1024x1024, {spp} spp, depth 8, NEE + "
                                    f"Russian roulette after depth 3, {args.scheduler} scheduler",
                        "l2": "flushed between steps"},
-            "mrays_per_s": round(segs * args.steps / sec / 1e6, 2), "segments_per_frame": segs}
+            "mrays_per_s": round(segs * args.steps / sec / 1e6, 2), "segments_per_frame": segs, "cpu_baseline": cpu}
     print(json.dumps(line), flush=True)
 
 
