@@ -64,3 +64,24 @@ def test_autotuner_picks_a_valid_shape_and_keeps_results():
     for sc, p, (o8, of) in zip(scs, params, outs):
         img, rad = alone(sc, p)
         np.testing.assert_array_equal(of.cpu().numpy(), rad)
+
+
+@pytest.mark.slow
+def test_full_batch_workload_equals_single_scene_frames():
+    """The benchmark's 64-scene batch (34.8M pixels; here at 1 spp to keep it
+    short): every scene's frame from the one persistent launch equals that
+    scene rendered alone, bit for bit."""
+    items = scenes.batch_workload(64, seed=0, spp=1)
+    scs, params, outs = [], [], []
+    for i, (mesh, st) in enumerate(items):
+        scs.append(native.Scene.from_setup(mesh, st))
+        params.append(native.pt_params(st, seed=i, mode=native.PT_KAJIYA))
+        outs.append((torch.empty((st.height, st.width, 3), dtype=torch.uint8, device="cuda"),
+                     torch.empty((st.height, st.width, 3), dtype=torch.float32, device="cuda")))
+    b = native.Batch(scs, params, outs)
+    b.render()
+    torch.cuda.synchronize()
+    for sc, p, (o8, of) in zip(scs, params, outs):
+        img, rad = alone(sc, p)
+        np.testing.assert_array_equal(of.cpu().numpy().view(np.uint32), rad.view(np.uint32))
+        np.testing.assert_array_equal(o8.cpu().numpy(), img)

@@ -162,3 +162,14 @@ def test_denoiser_table_matches_oracle(oracle):
     from nostrum_pray_gb300 import denoise
     assert denoise.num_params() == int(oracle.lib().orc_unet_num_params()) == 1_016_419
     assert denoise.forward_flops(512, 512) == 47_563_407_360
+
+
+def test_denoiser_fallback_sample_count():
+    """The fallback render's sample count: the smallest count whose plain
+    renders met the target on every calibration room, else the largest tried."""
+    from nostrum_pray_gb300 import denoise
+    curves = [[(4, 0.05, 1.0), (8, 0.009, 2.0), (16, 0.004, 4.0)],
+              [(4, 0.08, 1.0), (8, 0.02, 2.0), (16, 0.008, 4.0)]]
+    assert denoise.fallback_spp_from(curves, 0.01) == 16
+    assert denoise.fallback_spp_from(curves, 0.03) == 8
+    assert denoise.fallback_spp_from(curves, 0.001) == 16

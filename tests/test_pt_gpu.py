@@ -192,3 +192,32 @@ def test_auto_scheduler_gives_the_same_frames():
     a = sc.render_pt_host(native.pt_params(st, spp=32, max_depth=4, seed=2, scheduler=native.SCHED_AUTO))[1]
     b = sc.render_pt_host(native.pt_params(st, spp=32, max_depth=4, seed=2, scheduler=native.SCHED_PIXEL))[1]
     np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.slow
+def test_full_size_room_schedulers_and_chunks_agree():
+    """At the benchmark's size (the 101k-triangle room at 1024 x 1024, NEE +
+    RR, depth 8), properties that hold at any size: the wavefront and the
+    per-pixel schedulers give the same radiance bit for bit, and FP64 sums
+    accumulated over two sample ranges equal one call over both."""
+    m = scenes.room()
+    st = scenes.room_setup(1024, 1024)
+    sc = native.Scene.from_setup(m, st)
+    rads = []
+    for sched in (native.SCHED_PIXEL, native.SCHED_WAVEFRONT):
+        rad = torch.empty((1024, 1024, 3), dtype=torch.float32, device="cuda")
+        sc.render_pt(native.pt_params(st, spp=8, max_depth=8, seed=3, mode=native.PT_NEE, rr_depth=3,
+                                      scheduler=sched), None, rad)
+        rads.append(rad.cpu().numpy())
+    np.testing.assert_array_equal(rads[0].view(np.uint32), rads[1].view(np.uint32))
+    one = torch.zeros((1024, 1024, 3), dtype=torch.float64, device="cuda")
+    two = torch.zeros_like(one)
+    p = lambda spp, off: native.pt_params(st, spp=spp, max_depth=8, seed=3, mode=native.PT_NEE, rr_depth=3,
+                                          scheduler=native.SCHED_WAVEFRONT, sample_offset=off)
+    sc.accumulate_pt(p(8, 0), one)
+    sc.accumulate_pt(p(3, 0), two)
+    sc.accumulate_pt(p(5, 3), two)
+    torch.cuda.synchronize()
+    assert torch.equal(one, two)
+    # the mean of the FP64 sums is the radiance of the 8-sample frame up to FP32 rounding
+    np.testing.assert_allclose((one / 8).cpu().numpy(), rads[0], rtol=1e-5, atol=1e-6)
