@@ -587,14 +587,22 @@ cudaError_t tc_conv_plan(TcConvPlan &p, const __nv_bfloat16 *x, int n, int h, in
     size_t smem;
     int cols = 32;
     if (p.persistent) {
-        // a ring of three halos when it fits, else two
-        const int ring = 3 * halo + 9 * wtap + 128 <= kSmemPersistent ? 3 : 2;
+        while (cols < 2 * ((p.npad + 31) & ~31)) cols <<= 1;
+        // a ring of three halos unless two keep more CTAs resident per SM
+        auto ring_smem = [&](int ring) {
+            const size_t bar = (ring * halo + 9 * wtap + 15) & ~(size_t)15;
+            return bar + 8 * (2 * (size_t)ring + 6) + 32;
+        };
+        auto resident = [&](int ring) {
+            const size_t by_smem = kSmemPerSm / (ring_smem(ring) + 1024), by_tmem = 512 / (size_t)cols;
+            return by_smem < by_tmem ? by_smem : by_tmem;
+        };
+        const int ring = ring_smem(3) <= kSmemPersistent && resident(3) >= resident(2) ? 3 : 2;
         p.stages = ring;
         p.halo_stride = (uint32_t)halo;
         p.w_off = (uint32_t)(ring * halo);
         p.bar_off = (uint32_t)((ring * halo + 9 * wtap + 15) & ~(size_t)15);
-        smem = p.bar_off + 8 * (2 * (size_t)ring + 6) + 32;
-        while (cols < 2 * ((p.npad + 31) & ~31)) cols <<= 1;
+        smem = ring_smem(ring);
     } else {
         p.halo_stride = 0;
         p.w_off = (uint32_t)halo;
