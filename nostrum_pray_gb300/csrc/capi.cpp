@@ -460,6 +460,7 @@ pray_status pray_scene_create(const float *verts, const float *colors, const uin
         if (!validate_device_image(img, bad, &s->device_depth))
             return set_error(PRAY_ERR_UNSUPPORTED, "device layout: " + bad);
         gnodes.swap(img.nodes);
+        gnodes.insert(gnodes.end(), img.nodes_tight.begin(), img.nodes_tight.end());  // both copies, one buffer
         gtris.swap(img.tris);
         s->refined_leaves = img.refined_leaves;
         gshade.resize(n);
@@ -532,7 +533,7 @@ pray_status pray_scene_create(const float *verts, const float *colors, const uin
         }
         s->n_emit = (uint32_t)gemit.size();
     }
-    s->n_gnodes = (uint32_t)gnodes.size();
+    s->n_gnodes = (uint32_t)(gnodes.size() / 2);
     s->device_bytes = nb + tb + sb + gemit.size() * (sizeof(GTri) + sizeof(float));
     *out = s.release();
     return PRAY_OK;

@@ -47,7 +47,8 @@ struct alignas(16) GShade {
 
 // Launch-time view of a device scene.
 struct DevScene {
-    const GNode *nodes;
+    const GNode *nodes;  // n_nodes nodes with the reference's boxes, then the culling copy (same topology,
+                         // interior boxes bounding their triangles; for finite-direction rays)
     const GTri *tris;
     const GShade *shade;
     uint32_t n_nodes, n_refs, n_tris;

@@ -20,11 +20,16 @@ struct Item {
     uint32_t tri;  // triangle id
 };
 
+struct Tight {
+    float lo[3], hi[3];
+};
+
 struct Flattener {
     const BuiltTree &t;
     const std::vector<TriPre> &pre;
     int refine;
     DeviceImage &out;
+    std::vector<std::pair<uint32_t, Tight>> tight{};  // interior reference nodes: slot, padded triangle bounds
 
     uint32_t alloc_pair() {
         const uint32_t pair = (uint32_t)out.nodes.size();
@@ -52,13 +57,15 @@ struct Flattener {
         for (size_t i = lo; i < hi; i++) put_tri(items[i]);
     }
 
-    // Padded bounds of the triangles items[lo, hi).
+    // Padded bounds of the triangles items[lo, hi); an empty range gives the
+    // empty box (+inf, -inf), unpadded, which a union ignores.
     void padded_box(const std::vector<Item> &items, size_t lo, size_t hi, float blo[3], float bhi[3]) {
         for (int k = 0; k < 3; k++) blo[k] = INFINITY, bhi[k] = -INFINITY;
         for (size_t i = lo; i < hi; i++) {
             const Aabb &b = pre[items[i].tri].box;
             for (int k = 0; k < 3; k++) blo[k] = std::min(blo[k], b.lo[k]), bhi[k] = std::max(bhi[k], b.hi[k]);
         }
+        if (lo >= hi) return;
         for (int k = 0; k < 3; k++) {
             const float pad = (std::fabs(blo[k]) + std::fabs(bhi[k]) + (bhi[k] - blo[k])) * kPadRel + 1e-30f;
             blo[k] -= pad;
@@ -109,7 +116,9 @@ struct Flattener {
     }
 
     // Reference node p into slot (the box is the reference's, unpadded).
-    void put(int32_t p, uint32_t slot, int depth) {
+    // Returns the padded bounds of the triangles below it; for an interior
+    // node they are recorded in tight[slot].
+    Tight put(int32_t p, uint32_t slot, int depth) {
         const FlatNode &n = t.nodes[p];
         GNode g;
         for (int k = 0; k < 3; k++) g.lo[k] = n.box.lo[k], g.hi[k] = n.box.hi[k];
@@ -118,22 +127,28 @@ struct Flattener {
         if (n.left < 0) {
             std::vector<Item> items(n.count);
             for (uint32_t i = 0; i < n.count; i++) items[i] = Item{n.first + i, t.refs[n.first + i]};
+            Tight b;
+            padded_box(items, 0, items.size(), b.lo, b.hi);
             if (refine <= 0 || (int64_t)n.count <= refine || depth >= kMaxDeviceDepth) {
                 linear_leaf(g, items, 0, items.size());
                 out.nodes[slot] = g;
-                return;
+                return b;
             }
             out.refined_leaves++;
             out.nodes[slot] = g;
             const uint32_t pair = split_pair(items, 0, items.size(), depth);
             out.nodes[slot].a = pair;
-            return;
+            return b;
         }
         out.nodes[slot] = g;
         const uint32_t pair = alloc_pair();
         out.nodes[slot].a = pair;
-        put(n.left, pair, depth + 1);
-        put(n.right, pair + 1, depth + 1);
+        const Tight l = put(n.left, pair, depth + 1);
+        const Tight r = put(n.right, pair + 1, depth + 1);
+        Tight b;
+        for (int k = 0; k < 3; k++) b.lo[k] = std::min(l.lo[k], r.lo[k]), b.hi[k] = std::max(l.hi[k], r.hi[k]);
+        tight.push_back({slot, b});
+        return b;
     }
 };
 
@@ -147,6 +162,25 @@ void flatten_for_device(const BuiltTree &t, const std::vector<TriPre> &pre, int 
     out.sub_nodes = 0;
     Flattener f{t, pre, leaf_refine, out};
     f.put(0, 0, 0);
+    // the culling copy: same topology; an interior reference node takes the
+    // padded bounds of its triangles where they are smaller (by surface area,
+    // the chance a ray crosses them) than the reference's box. Either box alone
+    // culls conservatively for finite-direction rays; triangle bounds win for
+    // fine meshes in voxels with empty space, voxels for coarse meshes whose
+    // straddling triangles reach far outside them.
+    auto area = [](const float lo[3], const float hi[3]) {
+        const double x = (double)hi[0] - lo[0], y = (double)hi[1] - lo[1], z = (double)hi[2] - lo[2];
+        return x * y + y * z + z * x;
+    };
+    out.nodes_tight = out.nodes;
+    for (const auto &[slot, b] : f.tight) {
+        bool usable = true;  // finite and non-empty (no triangles below: keep the reference's box)
+        for (int k = 0; k < 3; k++)
+            usable = usable && std::isfinite(b.lo[k]) && std::isfinite(b.hi[k]) && b.lo[k] <= b.hi[k];
+        GNode &g = out.nodes_tight[slot];
+        if (!usable || !(area(b.lo, b.hi) < area(g.lo, g.hi))) continue;
+        for (int k = 0; k < 3; k++) g.lo[k] = b.lo[k], g.hi[k] = b.hi[k];
+    }
 }
 
 bool validate_device_image(const DeviceImage &img, std::string &why, int *max_depth) {

@@ -11,6 +11,19 @@
 // triangle record keeps its depth-first position in the reference's leaf order
 // as the tie-break key, so the refined leaves return the same triangle as a
 // linear scan in the reference's order.
+//
+// A second copy of the nodes (nodes_tight) has the same topology, but an
+// interior node of the reference's tree carries the padded bounds of the
+// triangles below it instead of the reference's box (for the SAH tree, a
+// voxel with much empty space) wherever those bounds have the smaller surface
+// area. Leaves keep the reference's box. It is used
+// for rays whose inverse direction is finite: for them the reference's slab
+// test is monotone in the box (a box inside another gives an interval inside
+// the other's), and the reference's boxes are nested, so the reference
+// reaches a leaf exactly when the leaf's own box passes; an interior box then
+// only needs to keep every triangle the ray can hit, which either the
+// reference's box or the padded triangle bounds do. Rays with an infinite
+// inverse component (NaN cases of the reference's test) use the exact copy.
 #pragma once
 
 #include <cstdint>
@@ -24,7 +37,8 @@
 namespace pray_gpu {
 
 struct DeviceImage {
-    std::vector<GNode> nodes;
+    std::vector<GNode> nodes;        // reference boxes (exact slab decisions)
+    std::vector<GNode> nodes_tight;  // same topology; interior reference nodes bound their triangles (padded)
     std::vector<GTri> tris;
     uint64_t refined_leaves = 0;  // reference leaves split into a sub-hierarchy
     uint64_t sub_nodes = 0;       // nodes added by the refinement

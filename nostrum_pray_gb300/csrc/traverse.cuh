@@ -153,6 +153,7 @@ __device__ __forceinline__ bool pop_node(const uint32_t *stk_a, const uint32_t *
 // src/pray.cpp:42).
 struct Trav {
     uint32_t a, b, la, lb;
+    uint32_t node_off;  // 0: the reference's boxes; n_nodes: the culling copy (finite inverse direction)
     float cur_tn, leaf_tn, limit, back, best_t;
     int best, sp;
     uint32_t best_key;
@@ -180,9 +181,11 @@ __device__ __forceinline__ void trav_start(const DevScene &s, const RayF &r, flo
     T.have_node = T.have_leaf = false;
     T.sp = 0;
     T.finite = isfinite(r.ix) && isfinite(r.iy) && isfinite(r.iz);
+    T.node_off = T.finite ? s.n_nodes : 0u;
     if (valid) {
         float tn, tf;
-        const float4 rlo = ldg4(s.nodes[0].lo), rhi = ldg4(s.nodes[0].hi);
+        const GNode *root = s.nodes + T.node_off;
+        const float4 rlo = ldg4(root->lo), rhi = ldg4(root->hi);
         if (slab(rlo, rhi, r, tn, tf)) {
             T.a = __float_as_uint(rlo.w);
             T.b = __float_as_uint(rhi.w);
@@ -203,7 +206,9 @@ __device__ __forceinline__ void trav_round(const DevScene &s, const RayF &r, flo
         if (!__any_sync(kFull, interior && !T.have_leaf)) break;
         if (interior) {
             if (kCount) fc->pairs++;
-            const GNode *c = s.nodes + T.a;
+            // finite inverse direction: culling boxes around the triangles (same
+            // topology; the reference's leaf boxes decide which leaves count)
+            const GNode *c = s.nodes + (T.a + T.node_off);
             const float4 l0 = ldg4(c[0].lo), h0 = ldg4(c[0].hi), l1 = ldg4(c[1].lo), h1 = ldg4(c[1].hi);
             float tn0, tf0, tn1, tf1;
             const bool v0 = slab(l0, h0, r, T.finite, tn0, tf0) && tn0 <= T.limit && tf0 >= T.back;
