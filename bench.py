@@ -537,12 +537,13 @@ def run_denoise_infer(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
             "config": {"workload": f"U-Net denoiser inference (19 3x3 convs, {D.num_params()} parameters, random "
                                    f"initialisation), one {res}x{res} frame: {cfg.spp_in}-spp room render + features",
-                       "tensor_cores": not args.dn_cuda_cores, "l2": "flushed between steps"},
+                       "tensor_cores": not args.dn_cuda_cores, "l2": "flushed between steps",
+                       "launch": "one CUDA graph per call (recorded by the first call)"},
             "e2e": {"value": round(args.steps / (e2e_ms / 1e3), 2), "unit": "frames/s",
                     "h2d_bytes_per_step": rad.numel() * 4 + feat.numel() * 2, "d2h_bytes_per_step": out.numel() * 4},
-            # per frame: input packing, 19 convolutions, 4 pools, 4 upsamplings, 4 concatenations,
-            # residual add, output transform
-            "gpu_launches": 34 * args.steps,
+            "gpu_launches": D.denoise_launches(res, res, tensor_cores=not args.dn_cuda_cores,
+                                               sm_count=torch.cuda.get_device_properties(0).multi_processor_count)
+            * args.steps,
             "roofline": {"bound": "tensor", "achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s",
                          "frac": round(achieved / peak, 5), "traffic": None, "peak_kind": peak_kind,
                          "algorithmic_flops_per_frame": flops,

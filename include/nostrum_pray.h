@@ -285,7 +285,11 @@ pray_status pray_denoiser_num_params(const pray_denoiser *d, uint64_t *n);
 pray_status pray_denoiser_get_params(const pray_denoiser *d, float *host);
 pray_status pray_denoiser_set_params(pray_denoiser *d, const float *host);
 /* Denoises n images of h x w (multiples of 16): radiance_dev n*h*w*3 floats,
- * features_dev n*h*w*7 FP16, out_dev n*h*w*3 floats (device pointers). */
+ * features_dev n*h*w*7 FP16, out_dev n*h*w*3 floats (device pointers),
+ * ordered after `stream`'s earlier work. The first call with a set of
+ * pointers and sizes runs its kernels on the stream and records them in a
+ * CUDA graph; a following call with the same pointers, sizes and kernel
+ * choice launches that graph. */
 pray_status pray_denoise(pray_denoiser *d, const float *radiance_dev, const uint16_t *features_dev, int32_t n,
                          int32_t h, int32_t w, float *out_dev, void *stream);
 /* One Adam step (lr; betas 0.9 / 0.999) on the L1 loss between the network

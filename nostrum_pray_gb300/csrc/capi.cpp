@@ -1012,8 +1012,7 @@ pray_status pray_denoise(pray_denoiser *d, const float *rad, const uint16_t *fea
     if (st != PRAY_OK) return st;
     cudaSetDevice(d->net.device);
     cudaStream_t s = (cudaStream_t)stream;
-    cudaError_t e = d->net.forward(rad, reinterpret_cast<const __half *>(feat), n, h, w, s);
-    if (e == cudaSuccess) e = d->net.output_radiance(out, s);
+    cudaError_t e = d->net.denoise(rad, reinterpret_cast<const __half *>(feat), n, h, w, out, s);
     return e == cudaSuccess ? PRAY_OK : cuda_error(e, "denoise");
 }
 

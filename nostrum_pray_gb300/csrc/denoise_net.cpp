@@ -47,6 +47,10 @@ cudaError_t dalloc(T *&p, size_t n) {
 Denoiser::~Denoiser() { release(); }
 
 void Denoiser::release() {
+    if (graph_) cudaGraphExecDestroy(graph_);
+    graph_ = nullptr;
+    if (capture_stream_) cudaStreamDestroy(capture_stream_);
+    capture_stream_ = nullptr;
     for (void *p : owned_) cudaFree(p);
     owned_.clear();
     act_.clear();
@@ -145,6 +149,7 @@ cudaError_t Denoiser::ensure(int n, int h, int w) {
     for (void *p : owned_)
         if (std::find(keep.begin(), keep.end(), p) == keep.end()) cudaFree(p);
     owned_ = keep;
+    generation_++;
     act_.clear();
     grad_.clear();
     n_ = n, h_ = h, w_dim_ = w;
@@ -340,6 +345,39 @@ cudaError_t Denoiser::apply_adam(float lr, cudaStream_t st) {
 
 cudaError_t Denoiser::output_radiance(float *out, cudaStream_t st) {
     return dn::expm1_out(out_, feat_, out, (size_t)n_ * h_ * w_dim_ * 3, st);
+}
+
+cudaError_t Denoiser::denoise(const float *rad, const __half *feat, int n, int h, int w, float *out,
+                              cudaStream_t st) {
+    GraphKey key;
+    key.rad = rad, key.feat = feat, key.out = out, key.n = n, key.h = h, key.w = w;
+    key.tensor_cores = tensor_cores_, key.generation = generation_;
+    if (graph_ && key == graph_key_) return cudaGraphLaunch(graph_, st);
+    // new buffers or sizes: run on the stream (allocating and planning as
+    // needed), then record the same launches for the calls that follow
+    cudaError_t e = forward(rad, feat, n, h, w, st);
+    if (e == cudaSuccess) e = output_radiance(out, st);
+    if (e != cudaSuccess) return e;
+    if (graph_) cudaGraphExecDestroy(graph_);
+    graph_ = nullptr;
+    if (!capture_stream_ && (e = cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking)) != cudaSuccess) {
+        capture_stream_ = nullptr;
+        return e;
+    }
+    if ((e = cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+    cudaError_t le = forward(rad, feat, n, h, w, capture_stream_);
+    if (le == cudaSuccess) le = output_radiance(out, capture_stream_);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(capture_stream_, &g);
+    if (le == cudaSuccess && e == cudaSuccess) e = cudaGraphInstantiate(&graph_, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (le != cudaSuccess || e != cudaSuccess) {
+        graph_ = nullptr;
+        return le != cudaSuccess ? le : e;
+    }
+    key.generation = generation_;
+    graph_key_ = key;
+    return cudaSuccess;
 }
 
 }  // namespace pray_gpu

@@ -29,6 +29,9 @@ class Denoiser {
     cudaError_t backward(const float *target, cudaStream_t st);
     cudaError_t apply_adam(float lr, cudaStream_t st);
     cudaError_t output_radiance(float *out, cudaStream_t st);
+    // forward + output_radiance; a call with the same buffers, sizes and
+    // kernel choice as the previous one replays them from a CUDA graph
+    cudaError_t denoise(const float *rad, const __half *feat, int n, int h, int w, float *out, cudaStream_t st);
     const float *loss_device() const { return loss_; }
     // forward convolutions on the tcgen05 tensor cores (default) or on the
     // CUDA cores
@@ -76,6 +79,24 @@ class Denoiser {
     const __half *feat_ = nullptr;  // features of the last forward (the caller's buffer; used until the call returns)
     int *err_ = nullptr;
     bool tensor_cores_ = true;
+    // the captured denoise call and what it was captured for; generation_
+    // counts reallocations of the activation buffers
+    struct GraphKey {
+        const float *rad = nullptr;
+        const __half *feat = nullptr;
+        float *out = nullptr;
+        int n = 0, h = 0, w = 0;
+        bool tensor_cores = false;
+        uint64_t generation = 0;
+        bool operator==(const GraphKey &o) const {
+            return rad == o.rad && feat == o.feat && out == o.out && n == o.n && h == o.h && w == o.w &&
+                   tensor_cores == o.tensor_cores && generation == o.generation;
+        }
+    };
+    GraphKey graph_key_{};
+    cudaGraphExec_t graph_ = nullptr;
+    cudaStream_t capture_stream_ = nullptr;
+    uint64_t generation_ = 0;
 };
 
 }  // namespace pray_gpu

@@ -64,6 +64,19 @@ def forward_flops(h: int, w: int, n: int = 1) -> int:
     return n * sum(2 * 9 * ci * co * (h >> l) * (w >> l) for ci, co, l in CONVS)
 
 
+def denoise_launches(h: int, w: int, n: int = 1, sm_count: int = 152, tensor_cores: bool = True) -> int:
+    """Kernels one pray_denoise call launches: input packing, 4 poolings, 4
+    upsample-concatenations, the 19 convolutions, the residual add and the
+    output transform. On the tensor cores a convolution with fewer than two
+    16x8-pixel tiles per SM splits its taps and adds a finalize kernel (the
+    rule of tc_conv_plan in csrc/denoise_tc.cu)."""
+    convs = 0
+    for _, _, l in CONVS:
+        tiles = n * -(-(w >> l) // 8) * -(-(h >> l) // 16)
+        convs += 2 if tensor_cores and tiles < 2 * sm_count else 1
+    return 1 + 4 + 4 + convs + 2
+
+
 def _setup(cfg: DenoiseConfig, res: Optional[int] = None):
     r = res or cfg.res
     return scenes.room_setup(r, r, spp=cfg.spp_in, max_depth=cfg.depth)

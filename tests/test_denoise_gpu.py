@@ -132,6 +132,47 @@ def test_tensor_core_forward_matches_cuda_cores(shape):
     assert rel(corr[1], corr[0]) < 2e-2
 
 
+@pytest.mark.parametrize("tensor_cores", [True, False])
+def test_denoise_graph_replays(tensor_cores):
+    """pray_denoise records its launches in a CUDA graph on the first call
+    with a set of buffers and replays the graph after. Replays equal the first
+    (stream-launched) call bit for bit, read new contents of the same buffers
+    and new weights (training steps at the same size and at another size, the
+    latter reallocating the activations), and new buffers record a new graph;
+    each result equals a fresh denoiser's first call with the same weights."""
+    den = native.Denoiser(seed=11)
+    den.set_tensor_cores(tensor_cores)
+    n, h, w = 1, 64, 48
+    rad, feat, tgt = random_batch(6, n, h, w)
+    t = lambda a: torch.from_numpy(a).cuda()
+    rad_t, feat_t, tgt_t = t(rad), t(feat), t(tgt)
+    out = torch.empty((n, h, w, 3), dtype=torch.float32, device="cuda")
+
+    def run(d, r, o):
+        d.denoise(r, feat_t, o)
+        d.check()
+        return o.cpu().numpy().copy()
+
+    def fresh(r):
+        f = native.Denoiser(seed=0)
+        f.set_tensor_cores(tensor_cores)
+        f.set_params(den.get_params())
+        return run(f, r, torch.empty_like(out))
+
+    first = run(den, rad_t, out)
+    np.testing.assert_array_equal(run(den, rad_t, out), first)
+    rad_t.copy_(t(random_batch(7, n, h, w)[0]))
+    np.testing.assert_array_equal(run(den, rad_t, out), fresh(rad_t))
+    den.train_step(rad_t, feat_t, tgt_t, 1e-3)
+    np.testing.assert_array_equal(run(den, rad_t, out), fresh(rad_t))
+    r2, f2, t2 = random_batch(8, 2, 32, 32)
+    den.train_step(t(r2), t(f2), t(t2), 1e-3)
+    np.testing.assert_array_equal(run(den, rad_t, out), fresh(rad_t))
+    out2 = torch.empty_like(out)
+    np.testing.assert_array_equal(run(den, rad_t, out2), fresh(rad_t))
+    assert not np.array_equal(first, out2.cpu().numpy())
+
+
 def test_trained_denoiser_beats_its_input():
     """What the learned part adds: trained on a few rooms rendered by the path
     tracer (4 spp inputs, 512-spp FP64 references), the denoiser lowers the
