@@ -100,6 +100,7 @@ struct pray_scene {
     uint64_t refined_leaves = 0;
     int device_depth = 0;  // deepest node of the device hierarchy
     float tol = 0.f;
+    float cull_c[3] = {0.f, 0.f, 0.f}, cull_r2 = -1.f;
     uint64_t device_bytes = 0;
     // wavefront path tracer: scratch (path pool, queues), private stream,
     // events and the captured frame graph
@@ -127,6 +128,8 @@ struct pray_scene {
         v.n_tris = (uint32_t)n_tris;
         v.tol = tol;
         v.depth = (uint32_t)device_depth;
+        for (int k = 0; k < 3; k++) v.cull_c[k] = cull_c[k];
+        v.cull_r2 = cull_r2;
         v.emit_tris = d_emit;
         v.emit_cdf = d_emit_cdf;
         v.n_emit = n_emit;
@@ -461,6 +464,8 @@ pray_status pray_scene_create(const float *verts, const float *colors, const uin
             return set_error(PRAY_ERR_UNSUPPORTED, "device layout: " + bad);
         gnodes.swap(img.nodes);
         gnodes.insert(gnodes.end(), img.nodes_tight.begin(), img.nodes_tight.end());  // both copies, one buffer
+        for (int k = 0; k < 3; k++) s->cull_c[k] = img.cull_center[k];
+        s->cull_r2 = img.cull_radius2;
         gtris.swap(img.tris);
         s->refined_leaves = img.refined_leaves;
         gshade.resize(n);

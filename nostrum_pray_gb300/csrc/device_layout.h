@@ -47,13 +47,15 @@ struct alignas(16) GShade {
 
 // Launch-time view of a device scene.
 struct DevScene {
-    const GNode *nodes;  // n_nodes nodes with the reference's boxes, then the culling copy (same topology,
-                         // interior boxes bounding their triangles; for finite-direction rays)
+    const GNode *nodes;  // n_nodes nodes with the reference's boxes and linear leaves, then the culling
+                         // copy (same topology, refined leaves, interior boxes bounding their triangles;
+                         // for finite-direction rays whose origin is within cull_r2 of cull_c)
     const GTri *tris;
     const GShade *shade;
     uint32_t n_nodes, n_refs, n_tris;
     float tol;  // absolute distance tolerance for culling boxes behind the origin
     uint32_t depth;  // deepest node level of the hierarchy (root 0): a traversal pushes at most this many nodes
+    float cull_c[3], cull_r2;  // centre and squared radius of the region of origins served by the culling copy
     // emitting triangles (for next-event estimation): geometry as GTri (v0.w
     // = triangle id) and the inclusive prefix sums of their areas
     const GTri *emit_tris;

@@ -11,6 +11,18 @@ namespace pray_gpu {
 namespace {
 
 constexpr float kPadRel = 1.0f / 65536.0f;
+// Every padded box also grows by this fraction of the scene's diagonal D, and
+// only rays whose origin lies within kCullReach diagonals of the scene's
+// centre use padded boxes (the others take the exact copy). Float errors grow
+// with the distance travelled, not with a box's coordinates: for an origin at
+// distance R from the centre, each endpoint of a slab test errs by at most
+// 3u(R + D) (u = 2^-24), and a hit that Moeller-Trumbore reports can lie off
+// its triangle by about u(R + D) / (sin a sin b), a the triangle's smallest
+// angle and b the ray's angle to its plane. The pad, 2^8 u D, keeps such hits
+// inside their boxes for sin a sin b down to 1/50 at the reach limit (1/170
+// for origins inside the scene).
+constexpr float kPadScene = 1.0f / 65536.0f;
+constexpr float kCullReach = 4.0f;
 // deepest node the flattened hierarchy may have (the kernels' traversal stack
 // holds one entry per level)
 constexpr int kMaxDeviceDepth = kMaxTraversalDepth;
@@ -29,7 +41,9 @@ struct Flattener {
     const std::vector<TriPre> &pre;
     int refine;
     DeviceImage &out;
+    float pad_scene = 0.f;                            // kPadScene x the scene's diagonal
     std::vector<std::pair<uint32_t, Tight>> tight{};  // interior reference nodes: slot, padded triangle bounds
+    std::vector<std::pair<uint32_t, GNode>> linear{};  // refined reference leaves: slot, linear leaf over the same range
 
     uint32_t alloc_pair() {
         const uint32_t pair = (uint32_t)out.nodes.size();
@@ -67,7 +81,8 @@ struct Flattener {
         }
         if (lo >= hi) return;
         for (int k = 0; k < 3; k++) {
-            const float pad = (std::fabs(blo[k]) + std::fabs(bhi[k]) + (bhi[k] - blo[k])) * kPadRel + 1e-30f;
+            const float pad =
+                (std::fabs(blo[k]) + std::fabs(bhi[k]) + (bhi[k] - blo[k])) * kPadRel + pad_scene + 1e-30f;
             blo[k] -= pad;
             bhi[k] += pad;
         }
@@ -136,8 +151,14 @@ struct Flattener {
             }
             out.refined_leaves++;
             out.nodes[slot] = g;
+            const uint32_t first = (uint32_t)out.tris.size();
             const uint32_t pair = split_pair(items, 0, items.size(), depth);
             out.nodes[slot].a = pair;
+            // the sub-hierarchy's leaves hold the leaf's references, contiguous
+            GNode flat = g;
+            flat.a = first;
+            flat.b = kLeafFlag | (uint32_t)(out.tris.size() - first);
+            linear.push_back({slot, flat});
             return b;
         }
         out.nodes[slot] = g;
@@ -161,6 +182,14 @@ void flatten_for_device(const BuiltTree &t, const std::vector<TriPre> &pre, int 
     out.refined_leaves = 0;
     out.sub_nodes = 0;
     Flattener f{t, pre, leaf_refine, out};
+    const Aabb &root = t.nodes[0].box;
+    double d2 = 0.0;
+    for (int k = 0; k < 3; k++) d2 += ((double)root.hi[k] - root.lo[k]) * ((double)root.hi[k] - root.lo[k]);
+    const bool sized = !t.refs.empty() && std::isfinite(d2);
+    const float diag = sized ? (float)std::sqrt(d2) : 0.f;
+    f.pad_scene = diag * kPadScene;
+    for (int k = 0; k < 3; k++) out.cull_center[k] = sized ? 0.5f * (root.lo[k] + root.hi[k]) : 0.f;
+    out.cull_radius2 = sized ? (kCullReach * diag) * (kCullReach * diag) : -1.f;
     f.put(0, 0, 0);
     // the culling copy: same topology; an interior reference node takes the
     // padded bounds of its triangles where they are smaller (by surface area,
@@ -173,6 +202,9 @@ void flatten_for_device(const BuiltTree &t, const std::vector<TriPre> &pre, int 
         return x * y + y * z + z * x;
     };
     out.nodes_tight = out.nodes;
+    // the exact copy scans refined leaves linearly: no padded box decides
+    // anything for the rays that use it
+    for (const auto &[slot, g] : f.linear) out.nodes[slot] = g;
     for (const auto &[slot, b] : f.tight) {
         bool usable = true;  // finite and non-empty (no triangles below: keep the reference's box)
         for (int k = 0; k < 3; k++)
@@ -183,9 +215,10 @@ void flatten_for_device(const BuiltTree &t, const std::vector<TriPre> &pre, int 
     }
 }
 
-bool validate_device_image(const DeviceImage &img, std::string &why, int *max_depth) {
-    int deepest = 0;
-    const uint64_t nn = img.nodes.size(), nt = img.tris.size();
+namespace {
+
+bool validate_nodes(const std::vector<GNode> &nodes, uint64_t nt, std::string &why, int &deepest) {
+    const uint64_t nn = nodes.size();
     if (nn < 2) {
         why = "device image has no root";
         return false;
@@ -203,7 +236,7 @@ bool validate_device_image(const DeviceImage &img, std::string &why, int *max_de
             return false;
         }
         deepest = std::max(deepest, d);
-        const GNode &g = img.nodes[i];
+        const GNode &g = nodes[i];
         if (g.b & kLeafFlag) {
             const uint64_t cnt = g.b & ~kLeafFlag;
             if ((uint64_t)g.a + cnt > nt) {
@@ -225,6 +258,20 @@ bool validate_device_image(const DeviceImage &img, std::string &why, int *max_de
             todo.push_back({c, d + 1});
         }
     }
+    return true;
+}
+
+}  // namespace
+
+bool validate_device_image(const DeviceImage &img, std::string &why, int *max_depth) {
+    int deepest = 0;
+    if (img.nodes_tight.size() != img.nodes.size()) {
+        why = "node copies differ in size";
+        return false;
+    }
+    if (!validate_nodes(img.nodes, img.tris.size(), why, deepest) ||
+        !validate_nodes(img.nodes_tight, img.tris.size(), why, deepest))
+        return false;
     if (max_depth) *max_depth = deepest;
     return true;
 }

@@ -153,7 +153,7 @@ __device__ __forceinline__ bool pop_node(const uint32_t *stk_a, const uint32_t *
 // src/pray.cpp:42).
 struct Trav {
     uint32_t a, b, la, lb;
-    uint32_t node_off;  // 0: the reference's boxes; n_nodes: the culling copy (finite inverse direction)
+    uint32_t node_off;  // 0: the exact copy; n_nodes: the culling copy (finite inverse direction, near origin)
     float cur_tn, leaf_tn, limit, back, best_t;
     int best, sp;
     uint32_t best_key;
@@ -181,7 +181,8 @@ __device__ __forceinline__ void trav_start(const DevScene &s, const RayF &r, flo
     T.have_node = T.have_leaf = false;
     T.sp = 0;
     T.finite = isfinite(r.ix) && isfinite(r.iy) && isfinite(r.iz);
-    T.node_off = T.finite ? s.n_nodes : 0u;
+    const float cx = r.ox - s.cull_c[0], cy = r.oy - s.cull_c[1], cz = r.oz - s.cull_c[2];
+    T.node_off = (T.finite && cx * cx + cy * cy + cz * cz <= s.cull_r2) ? s.n_nodes : 0u;
     if (valid) {
         float tn, tf;
         const GNode *root = s.nodes + T.node_off;
@@ -206,8 +207,8 @@ __device__ __forceinline__ void trav_round(const DevScene &s, const RayF &r, flo
         if (!__any_sync(kFull, interior && !T.have_leaf)) break;
         if (interior) {
             if (kCount) fc->pairs++;
-            // finite inverse direction: culling boxes around the triangles (same
-            // topology; the reference's leaf boxes decide which leaves count)
+            // culling copy: boxes around the triangles (same topology; the
+            // reference's leaf boxes decide which leaves count)
             const GNode *c = s.nodes + (T.a + T.node_off);
             const float4 l0 = ldg4(c[0].lo), h0 = ldg4(c[0].hi), l1 = ldg4(c[1].lo), h1 = ldg4(c[1].hi);
             float tn0, tf0, tn1, tf1;

@@ -13,7 +13,8 @@ log(1 + radiance) space and Adam, on random crops.
 Evaluation on held-out rooms: relMSE (mean over pixels and channels of
 (x - r)^2 / (r^2 + 0.01), FP64 on the GPU) of the noisy input, the denoised
 image and plain renders at increasing sample counts; the time each needs to
-reach relMSE <= 0.01; and a fallback: when the predicted error of a denoised
+reach relMSE <= 0.01 (for plain rendering, the render at the smallest sample
+count that reaches it, found by bisection); and a fallback: when the predicted error of a denoised
 image (half the relMSE between the denoised results of two independent
 renders) exceeds the target, the image is re-rendered plainly at the sample
 count that reached the target on the training rooms.
@@ -170,6 +171,44 @@ def plain_curve(cfg: DenoiseConfig, sc, ref, room_seed: int, torch, spps=(4, 8, 
     return out
 
 
+def smallest_spp(curve, target: float, measure):
+    """Smallest sample count whose plain render meets the target, with its
+    relMSE and render time: bisection between the last count of the curve
+    above the target and the first at or below it; measure(spp) renders and
+    returns (relMSE, time). Renders of one seed share their leading samples
+    (sample k of a pixel draws from the stream (seed, pixel, k)), so the error
+    falls with the count up to noise. None when no count of the curve met the
+    target."""
+    ok = [i for i, (_, e, _) in enumerate(curve) if e <= target]
+    if not ok:
+        return None
+    i = ok[0]
+    lo = curve[i - 1][0] if i > 0 else 0
+    hi, e_hi, t_hi = curve[i]
+    while hi - lo > 1:
+        mid = (lo + hi) // 2
+        e, t = measure(mid)
+        if e <= target:
+            hi, e_hi, t_hi = mid, e, t
+        else:
+            lo = mid
+    return hi, e_hi, t_hi
+
+
+def plain_to_target(cfg: DenoiseConfig, sc, ref, room_seed: int, torch, curve):
+    """smallest_spp for a room, rendering as plain_curve does."""
+    st = _setup(cfg)
+    rad = torch.empty((cfg.res, cfg.res, 3), dtype=torch.float32, device="cuda")
+
+    def measure(spp):
+        p = _params(cfg, st, spp, seed=room_seed * 7 + 3)
+        sc.render_pt(p, None, rad)  # warm (graph capture)
+        t = timed(lambda: sc.render_pt(p, None, rad), torch)
+        return relmse(rad, ref, torch), t
+
+    return smallest_spp(curve, cfg.target, measure)
+
+
 def denoised_eval(cfg: DenoiseConfig, den, sc, ref, room_seed: int, torch):
     """Denoised relMSE, time (render + features + inference) and predicted
     error from two independent renders."""
@@ -206,11 +245,11 @@ def denoised_eval(cfg: DenoiseConfig, den, sc, ref, room_seed: int, torch):
 def evaluate(cfg: DenoiseConfig, den, eval_rooms, torch, fallback_spp: int) -> Dict:
     rows = []
     for seed, (sc, ref) in eval_rooms.items():
-        curve = plain_curve(cfg, sc, ref, seed, torch, spps=(4, 8, 16, 32, 64, 128, 256))
-        plain_ok = [(spp, e, t) for spp, e, t in curve if e <= cfg.target]
+        curve = plain_curve(cfg, sc, ref, seed, torch, spps=(1, 2, 4, 8, 16, 32, 64, 128, 256))
+        plain = plain_to_target(cfg, sc, ref, seed, torch, curve)
         d = denoised_eval(cfg, den, sc, ref, seed, torch)
-        t_plain = plain_ok[0][2] if plain_ok else float("nan")
-        spp_plain = plain_ok[0][0] if plain_ok else None
+        t_plain = plain[2] if plain else float("nan")
+        spp_plain = plain[0] if plain else None
         # fallback: predicted error above target -> plain render at the calibrated spp
         t_final, e_final, used_fallback = d["time_s"], d["relmse_denoised"], False
         if d["predicted"] > cfg.target:

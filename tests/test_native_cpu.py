@@ -173,3 +173,25 @@ def test_denoiser_fallback_sample_count():
     assert denoise.fallback_spp_from(curves, 0.01) == 16
     assert denoise.fallback_spp_from(curves, 0.03) == 8
     assert denoise.fallback_spp_from(curves, 0.001) == 16
+
+
+def test_plain_time_to_target_bisects():
+    """The plain renderer's time to the target comes from the smallest sample
+    count that meets it: bisection between the curve's last count above the
+    target and its first below, rendering only the counts in between."""
+    from nostrum_pray_gb300 import denoise
+    err = lambda spp: 0.1 / spp  # meets 0.01 from 10 spp
+    curve = [(s, err(s), s * 1e-3) for s in (1, 2, 4, 8, 16, 32)]
+    seen = []
+
+    def measure(spp):
+        seen.append(spp)
+        return err(spp), spp * 1e-3
+
+    assert denoise.smallest_spp(curve, 0.01, measure) == (10, 0.01, 10e-3)
+    assert seen == [12, 10, 9]
+    seen.clear()
+    assert denoise.smallest_spp(curve, 0.2, measure) == (1, 0.1, 1e-3) and not seen
+    assert denoise.smallest_spp(curve, 0.001, measure) is None and not seen
+    # the first count already meets it: bisect from zero
+    assert denoise.smallest_spp(curve[2:], 0.04, measure) == (3, 0.1 / 3, 3e-3)

@@ -204,3 +204,37 @@ def test_rays_through_vertices_and_edges(oracle):
         wid, wt = orc.trace(rays, eps)
         assert int((ids != wid.astype(np.int32)).sum()) == 0
         np.testing.assert_array_equal(ts.view(np.uint32), wt.view(np.uint32))
+
+
+@pytest.mark.parametrize("dist", [0.3, 1.5, 3.5, 6.0, 100.0, 3000.0])
+def test_distant_origins(oracle, dist):
+    """Rays from origins `dist` scene diagonals from the scene's centre (from
+    inside the scene to far beyond the reach of the padded culling boxes,
+    where the exact node copy serves them), aimed at a cluster of small
+    triangles next to the world origin inside a scene of large ones: the
+    float error of a slab test grows with the distance travelled, not with
+    the small boxes' coordinates."""
+    rng = np.random.default_rng(int(dist * 10))
+    small = scenes.soup(20_000, 7)
+    big = scenes.soup(300, 8, spread=0.05)
+    m = scenes.Mesh(np.concatenate([small.verts * np.float32(0.02), big.verts * np.float32(2) - np.float32(1)]),
+                    np.concatenate([small.colors, big.colors]), np.zeros(20_300, np.uint8))
+    st = scenes.room_setup(64, 64)
+    sc = native.Scene.from_setup(m, st)
+    orc = oracle.OracleScene.from_setup(m, st)
+    v = m.verts.reshape(-1, 3).astype(np.float64)
+    lo, hi = v.min(0), v.max(0)
+    centre, diag = (lo + hi) / 2, float(np.linalg.norm(hi - lo))
+    n = 60_000
+    u = rng.normal(size=(n, 3))
+    o = centre + dist * diag * u / np.linalg.norm(u, axis=1, keepdims=True)
+    tgt = np.where((rng.random(n) < 0.7)[:, None], rng.uniform(-0.001, 0.021, (n, 3)), rng.uniform(lo, hi, (n, 3)))
+    o = o.astype(np.float32)
+    d = (tgt - o.astype(np.float64))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    rays = np.concatenate([o, d, (1.0 / d).astype(np.float32)], 1)
+    ids, ts = trace(sc, rays, 0.0)
+    wid, wt = orc.trace(rays, 0.0)
+    assert (wid >= 0).sum() > n // 3
+    assert int((ids != wid.astype(np.int32)).sum()) == 0
+    np.testing.assert_array_equal(ts.view(np.uint32), wt.view(np.uint32))
