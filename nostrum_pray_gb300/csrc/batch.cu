@@ -25,7 +25,9 @@ namespace {
 
 using namespace dev;
 
-template <int kStackN>
+// kLanes: every item runs mode 0, on the per-lane state machine; otherwise
+// each tile runs pt_pixel_sync (modes 0 and 1).
+template <int kStackN, bool kLanes>
 __global__ void __launch_bounds__(256, 4) k_batch_pt(BatchLaunch B) {
     constexpr unsigned kFull = 0xFFFFFFFFu;
     const uint32_t lane = threadIdx.x & 31u;
@@ -48,7 +50,13 @@ __global__ void __launch_bounds__(256, 4) k_batch_pt(BatchLaunch B) {
         const uint32_t py = (uint32_t)(local / tiles_x) * B.tile_h + lane / B.tile_w;
         const bool active = px < it.L.cam.width && py < it.L.cam.height;
         uint32_t segments = 0;
-        pt_pixel<kStackN>(it.s, it.L, active, px, py, segments);
+        if (kLanes) {
+            OnePixel src{active, px, py, false};
+            uint32_t pixels = 0;
+            pt_lanes<kStackN>(it.s, it.L, src, segments, pixels);
+        } else {
+            pt_pixel_sync<kStackN>(it.s, it.L, active, px, py, segments);
+        }
         count_paths(B.counters, active, it.L.num_samples, segments);
     }
 }
@@ -59,17 +67,22 @@ cudaError_t launch_batch_pt(const BatchLaunch &B, int block_threads, int blocks,
                             cudaStream_t stream) {
     cudaError_t e = cudaMemsetAsync(B.next_tile, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
-    if (stack_entries <= 32)
-        k_batch_pt<32><<<blocks, block_threads, 0, stream>>>(B);
-    else
-        k_batch_pt<kStack><<<blocks, block_threads, 0, stream>>>(B);
+    if (stack_entries <= 32) {
+        if (B.kajiya) k_batch_pt<32, true><<<blocks, block_threads, 0, stream>>>(B);
+        else k_batch_pt<32, false><<<blocks, block_threads, 0, stream>>>(B);
+    } else {
+        if (B.kajiya) k_batch_pt<kStack, true><<<blocks, block_threads, 0, stream>>>(B);
+        else k_batch_pt<kStack, false><<<blocks, block_threads, 0, stream>>>(B);
+    }
     return cudaGetLastError();
 }
 
-cudaError_t batch_max_blocks_per_sm(int block_threads, int stack_entries, int *blocks) {
+cudaError_t batch_max_blocks_per_sm(int block_threads, int stack_entries, bool kajiya, int *blocks) {
     if (stack_entries <= 32)
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_batch_pt<32>, block_threads, 0);
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_batch_pt<kStack>, block_threads, 0);
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            blocks, kajiya ? k_batch_pt<32, true> : k_batch_pt<32, false>, block_threads, 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        blocks, kajiya ? k_batch_pt<kStack, true> : k_batch_pt<kStack, false>, block_threads, 0);
 }
 
 }  // namespace pray_gpu

@@ -700,6 +700,7 @@ struct pray_batch {
     uint64_t total_tiles = 0;
     int max_depth = 0;
     int sm_count = 0;
+    bool kajiya = true;  // every item runs PRAY_PT_KAJIYA
     pray_batch_config cfg{8, 4, 128, 0, 64};
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
@@ -759,7 +760,8 @@ pray_status upload_batch(pray_batch *b) {
 
 int batch_blocks(pray_batch *b, const pray_batch_config &c) {
     int per_sm = 0;
-    if (batch_max_blocks_per_sm(c.block_threads, c.stack_entries, &per_sm) != cudaSuccess || per_sm < 1) per_sm = 1;
+    if (batch_max_blocks_per_sm(c.block_threads, c.stack_entries, b->kajiya, &per_sm) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
     if (c.blocks_per_sm > 0) per_sm = std::min(per_sm, c.blocks_per_sm);
     return per_sm * std::max(1, b->sm_count);
 }
@@ -773,6 +775,7 @@ BatchLaunch batch_view(const pray_batch *b, unsigned long long *counters) {
     B.tile_w = (uint32_t)b->cfg.tile_w;
     B.tile_h = (uint32_t)b->cfg.tile_h;
     B.counters = counters;
+    B.kajiya = b->kajiya;
     return B;
 }
 
@@ -807,6 +810,7 @@ pray_status pray_batch_create(pray_scene *const *scenes, const pray_pt_params *p
         it.L.radiance = of;
         b->items.push_back(it);
         b->scenes.push_back(s);
+        b->kajiya = b->kajiya && p.mode == PRAY_PT_KAJIYA;
         b->max_depth = std::max(b->max_depth, s->device_depth);
     }
     cudaError_t e = cudaSetDevice(b->device);

@@ -1,7 +1,7 @@
 // Per-pixel path tracing shared by the per-pixel kernel (pt.cu) and the
 // batched persistent kernel (batch.cu): one lane per pixel, the pixel's
 // samples in order, each an iterative bounce loop; all lanes of a warp call
-// pt_pixel together (the traversals are warp-collective).
+// these functions together (the traversals are warp-collective).
 //
 // Mode 0 restates the reference's Kajiya path tracer
 // (evaluatePathRecursive, src/pray.cpp:342-364; evaluatePath,
@@ -53,14 +53,18 @@ __device__ __forceinline__ uint32_t pick_emitter(const DevScene &s, float u) {
     return lo;
 }
 
-// All lanes of a warp call pt_pixel together (the traversals inside are
-// warp-collective). Each lane works through its own pixel's samples in order,
-// and starts its next sample as soon as its current path ends (path
-// regeneration) instead of waiting for the warp's longest path; the warp
-// loops while any lane still has a path. The per-pixel sums still add the
-// samples in sample order, so the result is unchanged.
+// Modes 0 and 1 bounce by bounce: all lanes of a warp call pt_pixel_sync
+// together and run each bounce's extension rays, then its next-event
+// occlusion rays, as two warp-collective traversals. Each lane works through
+// its own pixel's samples in order, and starts its next sample as soon as its
+// current path ends (path regeneration) instead of waiting for the warp's
+// longest path; the warp loops while any lane still has a path. The per-pixel
+// sums still add the samples in sample order, so the result is unchanged.
+// The per-pixel kernel runs it for modes 0 and 1, the batch kernel for mode 1
+// (next-event occlusion rays, all aimed at the emitters, keep the warp more
+// coherent traced together than mixed with bounce rays).
 template <int kStackN>
-__device__ __forceinline__ void pt_pixel(const DevScene &s, const PtLaunch &L, bool active, uint32_t px,
+__device__ __forceinline__ void pt_pixel_sync(const DevScene &s, const PtLaunch &L, bool active, uint32_t px,
                                          uint32_t py, uint32_t &segments) {
     constexpr unsigned kFull = 0xFFFFFFFFu;
     const uint64_t pixel = active ? (uint64_t)py * L.cam.width + px : 0;
@@ -203,6 +207,146 @@ __device__ __forceinline__ void pt_pixel(const DevScene &s, const PtLaunch &L, b
     }
 }
 
+// Pixels a lane takes one after another: a warp-collective source. All lanes
+// call take() together; a lane that asks (want) may receive a pixel.
+// OnePixel hands each lane one fixed pixel.
+struct OnePixel {
+    bool active;
+    uint32_t px, py;
+    bool given;
+    __device__ __forceinline__ bool drained() const { return given; }
+    __device__ __forceinline__ bool take(bool want, uint32_t &x, uint32_t &y) {
+        const bool got = want && !given && active;
+        given = true;
+        x = px, y = py;
+        return got;
+    }
+};
+
+// Mode 0 as a per-lane state machine (the batch kernel's: 355 against 296
+// Msamples/s on the 64-scene batch). All lanes of a warp call pt_lanes
+// together. Each lane holds one ray at a time, its path's current bounce, and
+// the warp advances every lane's ray by one traversal round (trav_round); a
+// lane whose ray is done shades the hit and starts its next ray before the
+// next round (the next bounce, the pixel's next sample, or a new pixel from
+// `src`), so lanes do not idle until the warp's slowest ray is done. Per lane
+// the operations and their order are those of the recursion, and the
+// per-pixel sums add the samples in sample order. pixels counts the pixels a
+// lane finished.
+template <int kStackN, class Src>
+__device__ __forceinline__ void pt_lanes(const DevScene &s, const PtLaunch &L, Src &src, uint32_t &segments,
+                                         uint32_t &pixels) {
+    constexpr unsigned kFull = 0xFFFFFFFFu;
+    const bool any_geometry = s.n_refs > 0;
+    float alb_r[kMaxPtDepth], alb_g[kMaxPtDepth], alb_b[kMaxPtDepth];
+    // the lane's pixel (its FP64 sums, when kept, are updated in place after
+    // each path)
+    bool have = false;
+    uint32_t px = 0, py = 0, smp = 0;
+    float sr = 0.f, sg = 0.f, sb = 0.f;
+    auto pixel = [&]() { return (uint64_t)py * L.cam.width + px; };
+    // its current path and ray
+    pray_pcg32 rng;
+    uint32_t depth = 0;
+    bool job = false;
+    RayF r{};
+    Trav T;
+    TravStack<kStackN> S;
+    T.have_node = T.have_leaf = false;
+    T.best = -1;
+
+    auto extend = [&](const RayF &ray) {
+        r = ray;
+        job = true;
+        trav_start<kClosest>(s, r, 0.f, any_geometry, T);
+    };
+    auto start_sample = [&]() {
+        rng = pray_pcg32_stream(L.seed, pixel(), L.sample_offset + smp);
+        depth = 0;
+        extend(primary_ray(L.cam, px, py));
+    };
+    // the path ended with value l: the albedos of its bounces are applied
+    // deepest first, and it joins the pixel's sums in sample order
+    auto end_path = [&](float lr, float lg, float lb) {
+        job = false;
+        while (depth > 0) {
+            depth--;
+            lr = lr * alb_r[depth], lg = lg * alb_g[depth], lb = lb * alb_b[depth];
+        }
+        sr = sr + lr, sg = sg + lg, sb = sb + lb;
+        if (L.sum64) {
+            double *a = L.sum64 + 3 * pixel();
+            a[0] = a[0] + (double)lr, a[1] = a[1] + (double)lg, a[2] = a[2] + (double)lb;
+        }
+        if (++smp < L.num_samples) {
+            start_sample();
+            return;
+        }
+        const float ns = (float)L.num_samples;
+        const float mr = sr / ns, mg = sg / ns, mb = sb / ns;
+        if (L.radiance) {
+            float *o = L.radiance + 3 * pixel();
+            o[0] = mr, o[1] = mg, o[2] = mb;
+        }
+        if (L.rgb) {
+            uint8_t *o = L.rgb + 3 * pixel();
+            o[0] = (uint8_t)quantise(smax(0.f, smin(1.f, mr)));
+            o[1] = (uint8_t)quantise(smax(0.f, smin(1.f, mg)));
+            o[2] = (uint8_t)quantise(smax(0.f, smin(1.f, mb)));
+        }
+        pixels++;
+        have = false;
+    };
+    // the ray is done: a miss returns the background, an emitter its colour,
+    // a hit at max_depth black; any other hit bounces
+    auto shade = [&]() {
+        const int pos = T.best;
+        if (pos < 0) {
+            end_path(L.bg[0], L.bg[1], L.bg[2]);
+            return;
+        }
+        const int id = (int)__float_as_uint(__ldg(&s.tris[pos].v0[3]));
+        const float4 nrm = shade_n(s, id), col = shade_c(s, id);
+        if (nrm.w != 0.f) {
+            end_path(col.x, col.y, col.z);
+            return;
+        }
+        if (depth >= L.max_depth) {
+            end_path(0.f, 0.f, 0.f);
+            return;
+        }
+        const float t = T.best_t;
+        const float hx = r.ox + r.dx * t, hy = r.oy + r.dy * t, hz = r.oz + r.dz * t;
+        alb_r[depth] = col.x, alb_g[depth] = col.y, alb_b[depth] = col.z;
+        const float u1 = pray_uniform(&rng), u2 = pray_uniform(&rng);
+        const float n3[3] = {nrm.x, nrm.y, nrm.z};
+        float d[3];
+        pray_sample_hemisphere(n3, u1, u2, d);
+        depth++;
+        extend(make_ray(hx, hy, hz, d[0], d[1], d[2]));
+    };
+
+    while (true) {
+        const unsigned idle = __ballot_sync(kFull, !have);
+        if (idle && !src.drained()) {
+            uint32_t x, y;
+            if (src.take(!have, x, y)) {
+                have = true;
+                px = x, py = y;
+                smp = 0;
+                sr = sg = sb = 0.f;
+                start_sample();
+            }
+        }
+        if (!__any_sync(kFull, job)) break;
+        trav_round<kClosest, false>(s, r, L.eps, 0.f, T, S, nullptr);
+        if (job && !T.active()) {
+            segments++;
+            shade();
+        }
+    }
+}
+
 // Mode 2 restates the reference's branching recursion
 // (evaluatePathRecursiveDiffuse, src/pray.cpp:315-340; its GPU twin
 // src/path_trace.cu:369-393): a miss returns the background, an emitter its
@@ -213,7 +357,7 @@ __device__ __forceinline__ void pt_pixel(const DevScene &s, const PtLaunch &L, b
 // finished ray's value is folded into its parent frame, and every frame whose
 // children are all done is folded into its own parent in turn. One PCG32
 // stream per pixel (sample index sample_offset) supplies the two uniforms of
-// each bounce in depth-first order. As in pt_pixel, every lane of a warp
+// each bounce in depth-first order. As in pt_pixel_sync, every lane of a warp
 // iterates until the warp's last tree ends, so the traversals line up.
 template <int kStackN>
 __device__ __forceinline__ void pt_pixel_diffuse(const DevScene &s, const PtLaunch &L, bool active, uint32_t px,

@@ -147,17 +147,21 @@ __device__ __forceinline__ bool pop_node(const uint32_t *stk_a, const uint32_t *
 // phase and one leaf phase for the whole warp, and a lane is done when
 // active() turns false.
 //
-// Closest hit (kAny = false): best = index of the winning triangle record or
-// -1, its distance in best_t. Any hit (kAny = true): best >= 0 once a
-// triangle with t > 0 and t * t < d2 is found (the occlusion test of
-// src/pray.cpp:42).
+// Closest hit: best = index of the winning triangle record or -1, its
+// distance in best_t. Any hit: best >= 0 once a triangle with t > 0 and
+// t * t < d2 is found (the occlusion test of src/pray.cpp:42). A traversal
+// looks for one or the other for the whole warp (kClosest, kAnyHit), or per
+// lane as Trav::any says (kPerLane: a warp mixing extension and occlusion
+// rays).
+enum TravMode { kClosest = 0, kAnyHit = 1, kPerLane = 2 };
+
 struct Trav {
     uint32_t a, b, la, lb;
     uint32_t node_off;  // 0: the exact copy; n_nodes: the culling copy (finite inverse direction, near origin)
     float cur_tn, leaf_tn, limit, back, best_t;
     int best, sp;
     uint32_t best_key;
-    bool have_node, have_leaf, finite;
+    bool have_node, have_leaf, finite, any;
     __device__ __forceinline__ bool active() const { return have_node || have_leaf; }
 };
 
@@ -169,12 +173,15 @@ struct TravStack {
     float t[kStackN];
 };
 
-template <bool kAny>
-__device__ __forceinline__ void trav_start(const DevScene &s, const RayF &r, float d2, bool valid, Trav &T) {
+// `any` (kPerLane only): this lane's ray looks for any occluder.
+template <int kMode>
+__device__ __forceinline__ void trav_start(const DevScene &s, const RayF &r, float d2, bool valid, Trav &T,
+                                           bool any = false) {
+    T.any = kMode == kAnyHit || (kMode == kPerLane && any);
     T.best_t = FLT_MAX;
     T.best = -1;
     T.best_key = 0xFFFFFFFFu;
-    T.limit = kAny ? sqrtf(d2) * kPruneRel : FLT_MAX;
+    T.limit = T.any ? sqrtf(d2) * kPruneRel : FLT_MAX;
     T.back = -s.tol;
     T.a = T.b = T.la = T.lb = 0;
     T.cur_tn = T.leaf_tn = 0.f;
@@ -196,11 +203,12 @@ __device__ __forceinline__ void trav_start(const DevScene &s, const RayF &r, flo
     }
 }
 
-template <bool kAny, bool kCount, int kStackN>
+template <int kMode, bool kCount, int kStackN>
 __device__ __forceinline__ void trav_round(const DevScene &s, const RayF &r, float eps, float d2, Trav &T,
                                            TravStack<kStackN> &S, FetchCount *fc) {
     static_assert(kStackN >= 2 && kStackN <= kStack, "stack entries");
     constexpr unsigned kFull = 0xFFFFFFFFu;
+    const bool any_hit = kMode == kAnyHit || (kMode == kPerLane && T.any);
     // 1. interior nodes, until every lane has found a leaf
     while (true) {
         const bool interior = T.have_node && !(T.b & kLeafFlag);
@@ -260,7 +268,7 @@ __device__ __forceinline__ void trav_round(const DevScene &s, const RayF &r, flo
                     const float4 v0 = ldg4(Tr->v0), e1 = ldg4(Tr->e1), e2 = ldg4(Tr->e2);
                     float t;
                     if (intersect_tri(v0, e1, e2, r, eps, t) && t > 0) {
-                        if (kAny) {
+                        if (any_hit) {
                             if (d2 > t * t) {
                                 T.best = (int)i;
                                 T.have_node = T.have_leaf = false;
@@ -287,10 +295,11 @@ __device__ __forceinline__ void trav_round(const DevScene &s, const RayF &r, flo
 template <bool kAny, bool kCount = false, int kStackN = kStack>
 __device__ __forceinline__ int traverse(const DevScene &s, const RayF &r, float eps, float d2, bool valid,
                                         float &best_t, FetchCount *fc = nullptr) {
+    constexpr int kMode = kAny ? kAnyHit : kClosest;
     Trav T;
     TravStack<kStackN> S;
-    trav_start<kAny>(s, r, d2, valid, T);
-    while (__any_sync(0xFFFFFFFFu, T.active())) trav_round<kAny, kCount>(s, r, eps, d2, T, S, fc);
+    trav_start<kMode>(s, r, d2, valid, T);
+    while (__any_sync(0xFFFFFFFFu, T.active())) trav_round<kMode, kCount>(s, r, eps, d2, T, S, fc);
     best_t = T.best_t;
     return T.best;
 }

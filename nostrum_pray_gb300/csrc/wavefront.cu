@@ -145,11 +145,11 @@ __global__ void __launch_bounds__(kThreads, kTraceBlocksPerSm) k_wf_extend(DevSc
                 r.dx = d.x, r.dy = d.y, r.dz = d.z;
                 r.ix = 1.0f / d.x, r.iy = 1.0f / d.y, r.iz = 1.0f / d.z;
                 has = true;
-                trav_start<false>(s, r, 0.f, s.n_refs > 0, T);
+                trav_start<kClosest>(s, r, 0.f, s.n_refs > 0, T);
             }
         }
         if (!__any_sync(kFull, has)) break;
-        trav_round<false, false>(s, r, L.eps, 0.f, T, S, nullptr);
+        trav_round<kClosest, false>(s, r, L.eps, 0.f, T, S, nullptr);
         if (has && !T.active()) {
             w.hit_t[p] = T.best_t;
             w.hit_ref[p] = T.best;
@@ -288,11 +288,11 @@ __global__ void __launch_bounds__(kThreads, kTraceBlocksPerSm) k_wf_occlude(DevS
                 r = make_ray(jo.x, jo.y, jo.z, jd.x, jd.y, jd.z);
                 d2 = jd.w;
                 has = true;
-                trav_start<true>(s, r, d2, s.n_refs > 0, T);
+                trav_start<kAnyHit>(s, r, d2, s.n_refs > 0, T);
             }
         }
         if (!__any_sync(kFull, has)) break;
-        trav_round<true, false>(s, r, L.eps, d2, T, S, nullptr);
+        trav_round<kAnyHit, false>(s, r, L.eps, d2, T, S, nullptr);
         if (has && !T.active()) {
             seg++;
             if (T.best < 0) {
