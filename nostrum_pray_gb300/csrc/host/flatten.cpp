@@ -217,7 +217,7 @@ void flatten_for_device(const BuiltTree &t, const std::vector<TriPre> &pre, int 
 
 namespace {
 
-bool validate_nodes(const std::vector<GNode> &nodes, uint64_t nt, std::string &why, int &deepest) {
+bool validate_nodes(const std::vector<GNode> &nodes, uint64_t nt, std::string &why, int &deepest, uint64_t &refs) {
     const uint64_t nn = nodes.size();
     if (nn < 2) {
         why = "device image has no root";
@@ -243,6 +243,7 @@ bool validate_nodes(const std::vector<GNode> &nodes, uint64_t nt, std::string &w
                 why = "leaf range out of bounds";
                 return false;
             }
+            refs += cnt;
             continue;
         }
         if (g.b != 0 || (g.a & 1u) || (uint64_t)g.a + 1 >= nn || g.a < 2) {
@@ -269,9 +270,15 @@ bool validate_device_image(const DeviceImage &img, std::string &why, int *max_de
         why = "node copies differ in size";
         return false;
     }
-    if (!validate_nodes(img.nodes, img.tris.size(), why, deepest) ||
-        !validate_nodes(img.nodes_tight, img.tris.size(), why, deepest))
+    uint64_t exact_refs = 0, cull_refs = 0;
+    if (!validate_nodes(img.nodes, img.tris.size(), why, deepest, exact_refs) ||
+        !validate_nodes(img.nodes_tight, img.tris.size(), why, deepest, cull_refs))
         return false;
+    // each copy reaches every triangle reference exactly once
+    if (exact_refs != img.tris.size() || cull_refs != img.tris.size()) {
+        why = "a node copy does not reach every triangle reference once";
+        return false;
+    }
     if (max_depth) *max_depth = deepest;
     return true;
 }

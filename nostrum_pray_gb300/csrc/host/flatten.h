@@ -57,8 +57,9 @@ struct DeviceImage {
 void flatten_for_device(const BuiltTree &t, const std::vector<TriPre> &pre, int leaf_refine, DeviceImage &out);
 
 // Structural check of both copies before upload: child pairs and leaf ranges
-// in bounds, each node reached once, depth within the kernels' traversal stack
-// (the deepest node's depth goes to *max_depth when given).
+// in bounds, each node reached once, every triangle reference reached once,
+// depth within the kernels' traversal stack (the deepest node's depth goes to
+// *max_depth when given).
 bool validate_device_image(const DeviceImage &img, std::string &why, int *max_depth = nullptr);
 
 }  // namespace pray_gpu
