@@ -5,6 +5,7 @@
 #include <cfloat>
 #include <cmath>
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <exception>
 #include <memory>
@@ -101,6 +102,7 @@ struct pray_scene {
     int device_depth = 0;  // deepest node of the device hierarchy
     float tol = 0.f;
     float cull_c[3] = {0.f, 0.f, 0.f}, cull_r2 = -1.f;
+    std::atomic<int> rt_packets{PRAY_TRAVERSAL_AUTO};  // pray_traversal of the ray-traced frames
     uint64_t device_bytes = 0;
     // wavefront path tracer: scratch (path pool, queues), private stream,
     // events and the captured frame graph
@@ -197,6 +199,40 @@ pray_status check_params(const pray_rt_params *p) {
         return set_error(PRAY_ERR_INVALID_ARGUMENT, "n_lights must be in [0, 64]");
     if (p->n_lights > 0 && !p->lights) return set_error(PRAY_ERR_INVALID_ARGUMENT, "lights is NULL");
     return PRAY_OK;
+}
+
+// A ray-traced frame with the scene's traversal. The first frame of a scene
+// renders with the per-lane and with the warp-packet traversal, twice each,
+// times the second of each pair and keeps the faster for the scene (the
+// frames are identical; coherent surfaces favour packets, depth-complex
+// triangle soups the per-lane walk); it synchronises `stream`.
+cudaError_t render_rt(pray_scene *s, RtLaunch L, cudaStream_t stream) {
+    if (s->rt_packets.load() < 0) {
+        RtLaunch C = L;
+        C.counters = nullptr;
+        C.count_fetches = 0;
+        cudaEvent_t ev[4] = {};
+        cudaError_t e = cudaSuccess;
+        for (cudaEvent_t &x : ev)
+            if (e == cudaSuccess) e = cudaEventCreate(&x);
+        for (int rep = 0; rep < 2 && e == cudaSuccess; rep++)
+            for (int m = 0; m < 2 && e == cudaSuccess; m++) {
+                C.packets = m;
+                if (rep == 1) e = cudaEventRecord(ev[2 * m], stream);
+                if (e == cudaSuccess) e = launch_render_rt(s->view(), C, stream);
+                if (rep == 1 && e == cudaSuccess) e = cudaEventRecord(ev[2 * m + 1], stream);
+            }
+        float ms[2] = {0.f, 0.f};
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev[3]);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[0], ev[0], ev[1]);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[1], ev[2], ev[3]);
+        for (cudaEvent_t x : ev)
+            if (x) cudaEventDestroy(x);
+        if (e != cudaSuccess) return e;
+        s->rt_packets.store(ms[1] < ms[0] ? 1 : 0);
+    }
+    L.packets = s->rt_packets.load();
+    return launch_render_rt(s->view(), L, stream);
 }
 
 pray_status check_pt_params(const pray_pt_params *p) {
@@ -552,6 +588,20 @@ pray_status pray_scene_destroy(pray_scene *s) {
     return PRAY_OK;
 }
 
+pray_status pray_scene_set_traversal(pray_scene *s, int32_t traversal) {
+    if (!s) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (traversal < PRAY_TRAVERSAL_AUTO || traversal > PRAY_TRAVERSAL_PACKETS)
+        return set_error(PRAY_ERR_INVALID_ARGUMENT, "traversal must be PRAY_TRAVERSAL_AUTO, _LANES or _PACKETS");
+    s->rt_packets.store(traversal);
+    return PRAY_OK;
+}
+
+pray_status pray_scene_traversal(const pray_scene *s, int32_t *traversal) {
+    if (!s || !traversal) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    *traversal = s->rt_packets.load();
+    return PRAY_OK;
+}
+
 pray_status pray_scene_stats(const pray_scene *s, uint64_t *out) {
     if (!s || !out) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
     tree_stats(s->tree, out);
@@ -586,7 +636,7 @@ pray_status pray_render_rt(pray_scene *s, const pray_rt_params *p, uint8_t *rgb,
     L.ids = ids;
     L.ts = ts;
     L.counters = counters;
-    e = launch_render_rt(s->view(), L, (cudaStream_t)stream);
+    e = render_rt(s, L, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_error(e, "render_rt launch");
     return PRAY_OK;
 }
@@ -604,7 +654,7 @@ pray_status pray_render_rt_host(pray_scene *s, const pray_rt_params *p, uint8_t 
     RtLaunch L = make_launch(p);
     L.rgb = s->d_rgb;
     L.counters = s->d_counters;
-    if ((e = launch_render_rt(s->view(), L, 0)) != cudaSuccess) return cuda_error(e, "render_rt launch");
+    if ((e = render_rt(s, L, 0)) != cudaSuccess) return cuda_error(e, "render_rt launch");
     if ((e = cudaMemcpy(rgb_host, s->d_rgb, bytes, cudaMemcpyDeviceToHost)) != cudaSuccess)
         return cuda_error(e, "cudaMemcpy (frame)");
     if (rays_cast) {
@@ -630,7 +680,7 @@ pray_status pray_render_rt_counts(pray_scene *s, const pray_rt_params *p, uint64
     L.rgb = s->d_rgb;
     L.counters = s->d_counters;
     L.count_fetches = 1;
-    if ((e = launch_render_rt(s->view(), L, 0)) != cudaSuccess) return cuda_error(e, "render_rt launch");
+    if ((e = render_rt(s, L, 0)) != cudaSuccess) return cuda_error(e, "render_rt launch");
     unsigned long long c[5];
     if ((e = cudaMemcpy(c, s->d_counters, sizeof(c), cudaMemcpyDeviceToHost)) != cudaSuccess)
         return cuda_error(e, "cudaMemcpy (counters)");

@@ -42,16 +42,22 @@ __global__ void __launch_bounds__(128) k_trace_closest(DevScene s, const float *
 // the quantisation of src/pray.cpp:576-588). Every lane of a warp runs the
 // same light loop so that the warp-collective traversals line up; a lane
 // whose colour saturated stops casting (the reference's early break).
-template <bool kCount, int kStackN>
+// kPacket: the warp traverses its tile's rays as a packet (traverse_coherent).
+template <bool kCount, int kStackN, bool kPacket>
 __global__ void __launch_bounds__(128, 8) k_render_rt(DevScene s, RtLaunch L) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t px, py;
     const bool active = pixel_of(i, L.cam.width, L.cam.height, px, py);
     uint32_t shadows = 0;
     FetchCount fc;
+    // one traversal stack per warp (the tile's rays are coherent)
+    __shared__ uint32_t stacks[4][3 * kStackN];
+    uint32_t *stk = stacks[threadIdx.x >> 5];
     const RayF r = primary_ray(L.cam, active ? px : 0, active ? py : 0);
     float dist = FLT_MAX;
-    const int pos = traverse<false, kCount, kStackN>(s, r, L.eps, 0.f, active && s.n_refs > 0, dist, &fc);
+    const bool geo = active && s.n_refs > 0;
+    const int pos = kPacket ? traverse_coherent<false, kCount, kStackN>(s, r, L.eps, 0.f, geo, dist, stk, &fc)
+                            : traverse<false, kCount, kStackN>(s, r, L.eps, 0.f, geo, dist, &fc);
     const bool hit = active && pos >= 0;
     float cr = L.bg[0], cg = L.bg[1], cb = L.bg[2];
     int32_t id = -1;
@@ -81,7 +87,9 @@ __global__ void __launch_bounds__(128, 8) k_render_rt(DevScene s, RtLaunch L) {
         const RayF sr = need ? make_ray(hx, hy, hz, lx, ly, lz) : r;
         shadows += need ? 1u : 0u;
         float dummy;
-        const bool occluded = traverse<true, kCount, kStackN>(s, sr, L.eps, d2, need, dummy, &fc) >= 0;
+        const bool occluded =
+            (kPacket ? traverse_coherent<true, kCount, kStackN>(s, sr, L.eps, d2, need, dummy, stk, &fc)
+                     : traverse<true, kCount, kStackN>(s, sr, L.eps, d2, need, dummy, &fc)) >= 0;
         if (need && !occluded) {
             const float w = 1.0f / d2;
             cr = cr + ((alb.x * L.lights[l][3]) * lambert) * w;
@@ -177,12 +185,13 @@ cudaError_t launch_render_rt(const DevScene &s, const RtLaunch &L, cudaStream_t 
     const unsigned bs = 128, grid = (unsigned)((threads + bs - 1) / bs);
     // a 32-entry stack (half the per-thread local memory) when the hierarchy is shallow enough
     const bool small = s.depth < 32;
+    auto go = [&](auto kernel) { kernel<<<grid, bs, 0, stream>>>(s, L); };
     if (L.count_fetches) {
-        if (small) k_render_rt<true, 32><<<grid, bs, 0, stream>>>(s, L);
-        else k_render_rt<true, kStack><<<grid, bs, 0, stream>>>(s, L);
+        if (L.packets) small ? go(k_render_rt<true, 32, true>) : go(k_render_rt<true, kStack, true>);
+        else small ? go(k_render_rt<true, 32, false>) : go(k_render_rt<true, kStack, false>);
     } else {
-        if (small) k_render_rt<false, 32><<<grid, bs, 0, stream>>>(s, L);
-        else k_render_rt<false, kStack><<<grid, bs, 0, stream>>>(s, L);
+        if (L.packets) small ? go(k_render_rt<false, 32, true>) : go(k_render_rt<false, kStack, true>);
+        else small ? go(k_render_rt<false, 32, false>) : go(k_render_rt<false, kStack, false>);
     }
     return cudaGetLastError();
 }

@@ -27,6 +27,7 @@ struct RtLaunch {
     float *ts;                       // optional out: primary hit distance per pixel (FLT_MAX: miss)
     unsigned long long *counters;    // optional out (accumulated): [0] primary rays, [1] occlusion rays
     int count_fetches;               // also accumulate [2] node-pair fetches, [3] triangle fetches, [4] shaded hits
+    int packets;                     // warp-packet traversal (traverse_packet) for warps that can take it
 };
 
 constexpr int kMaxPtDepth = 64;  // bounce limit of the path tracer (per-thread albedo stack)

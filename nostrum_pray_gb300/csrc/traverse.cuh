@@ -304,6 +304,131 @@ __device__ __forceinline__ int traverse(const DevScene &s, const RayF &r, float 
     return T.best;
 }
 
+// Warp-packet traversal for coherent rays (the primary and occlusion rays of
+// a pixel tile), after the packet traversals of Wald et al. (EG 2001) and
+// Garanzha & Loop (2010): the warp walks one node sequence of the culling
+// copy with a mask of the lanes whose own box tests passed, so node and
+// triangle loads are warp-uniform (one broadcast each) and the traversal
+// stack is one shared stack per warp (`stk`: 3 x kStackN words of shared
+// memory: node payload, lane mask) instead of one per lane. Every lane still
+// applies its own slab test (with its own pruning bound) to every box on its
+// way and its own triangle test to every reference of the leaves it reaches,
+// so it returns the same lexicographic minimum as traverse(); only the order
+// of visits differs (the warp enters first the child that is nearer for most
+// of the lanes entering both), and a lane whose bound shrank after a node was
+// pushed still visits it (testing a popped node's box again measured slower:
+// 2,571 against 2,682 Mrays/s on the 1.31M sphere). Only for warps whose
+// valid lanes all use the culling copy.
+template <bool kAny, bool kCount, int kStackN>
+__device__ __forceinline__ int traverse_packet(const DevScene &s, const RayF &r, float eps, float d2, bool valid,
+                                               float &best_t, uint32_t *stk, FetchCount *fc) {
+    constexpr unsigned kFull = 0xFFFFFFFFu;
+    const uint32_t lane = threadIdx.x & 31u;
+    const GNode *nodes = s.nodes + s.n_nodes;
+    float limit = kAny ? sqrtf(d2) * kPruneRel : FLT_MAX;
+    const float back = -s.tol;
+    best_t = FLT_MAX;
+    int best = -1;
+    uint32_t best_key = 0xFFFFFFFFu;
+    uint32_t a, b;
+    unsigned mask;
+    {
+        const float4 lo = ldg4(nodes[0].lo), hi = ldg4(nodes[0].hi);
+        float tn, tf;
+        mask = __ballot_sync(kFull, valid && slab(lo, hi, r, true, tn, tf));
+        a = __float_as_uint(lo.w);
+        b = __float_as_uint(hi.w);
+    }
+    int sp = 0;
+    while (mask) {
+        const bool in = (mask >> lane) & 1u;
+        if (!(b & kLeafFlag)) {
+            const GNode *c = nodes + a;
+            const float4 l0 = ldg4(c[0].lo), h0 = ldg4(c[0].hi), l1 = ldg4(c[1].lo), h1 = ldg4(c[1].hi);
+            if (kCount && in) fc->pairs++;
+            float tn0, tf0, tn1, tf1;
+            const bool v0 = in && slab(l0, h0, r, true, tn0, tf0) && tn0 <= limit && tf0 >= back;
+            const bool v1 = in && slab(l1, h1, r, true, tn1, tf1) && tn1 <= limit && tf1 >= back;
+            const unsigned m0 = __ballot_sync(kFull, v0), m1 = __ballot_sync(kFull, v1);
+            if (m0 && m1) {
+                const unsigned both = m0 & m1;
+                const unsigned near0 = __ballot_sync(kFull, v0 && v1 && tn0 <= tn1);
+                const bool go0 = both ? 2 * __popc(near0) >= __popc(both) : __popc(m0) >= __popc(m1);
+                if (lane == 0) {
+                    stk[sp] = __float_as_uint(go0 ? l1.w : l0.w);
+                    stk[kStackN + sp] = __float_as_uint(go0 ? h1.w : h0.w);
+                    stk[2 * kStackN + sp] = go0 ? m1 : m0;
+                }
+                sp++;
+                a = __float_as_uint(go0 ? l0.w : l1.w);
+                b = __float_as_uint(go0 ? h0.w : h1.w);
+                mask = go0 ? m0 : m1;
+                continue;
+            }
+            if (m0 | m1) {
+                a = __float_as_uint(m0 ? l0.w : l1.w);
+                b = __float_as_uint(m0 ? h0.w : h1.w);
+                mask = m0 | m1;
+                continue;
+            }
+        } else {
+            // the lanes in the mask test the leaf's references
+            bool open = in;
+            const uint32_t end = a + (b & ~kLeafFlag);
+            for (uint32_t i = a; i < end; i++) {
+                const GTri *Tr = s.tris + i;
+                const float4 v0 = ldg4(Tr->v0), e1 = ldg4(Tr->e1), e2 = ldg4(Tr->e2);
+                if (open) {
+                    if (kCount) fc->tris++;
+                    float t;
+                    if (intersect_tri(v0, e1, e2, r, eps, t) && t > 0) {
+                        if (kAny) {
+                            if (d2 > t * t) {
+                                best = (int)i;
+                                open = false;
+                            }
+                        } else {
+                            const uint32_t key = __float_as_uint(e1.w);
+                            if (t < best_t || (best >= 0 && t == best_t && key < best_key)) {
+                                best_t = t;
+                                best = (int)i;
+                                best_key = key;
+                                limit = t * kPruneRel;
+                            }
+                        }
+                    }
+                }
+                if (kAny && !__any_sync(kFull, open)) break;
+            }
+        }
+        // next node: the top of the stack, without the lanes already done
+        const unsigned done = kAny ? __ballot_sync(kFull, best >= 0) : 0u;
+        mask = 0;
+        __syncwarp();
+        while (sp > 0 && !mask) {
+            sp--;
+            a = stk[sp];
+            b = stk[kStackN + sp];
+            mask = stk[2 * kStackN + sp] & ~done;
+        }
+        __syncwarp();
+    }
+    return best;
+}
+
+// traverse_packet where every valid lane of the warp uses the culling copy,
+// else traverse(); all lanes of the warp call it together.
+template <bool kAny, bool kCount, int kStackN>
+__device__ __forceinline__ int traverse_coherent(const DevScene &s, const RayF &r, float eps, float d2, bool valid,
+                                                 float &best_t, uint32_t *stk, FetchCount *fc = nullptr) {
+    const bool finite = isfinite(r.ix) && isfinite(r.iy) && isfinite(r.iz);
+    const float cx = r.ox - s.cull_c[0], cy = r.oy - s.cull_c[1], cz = r.oz - s.cull_c[2];
+    const bool cull = finite && cx * cx + cy * cy + cz * cz <= s.cull_r2;
+    if (__all_sync(0xFFFFFFFFu, !valid || cull))
+        return traverse_packet<kAny, kCount, kStackN>(s, r, eps, d2, valid, best_t, stk, fc);
+    return traverse<kAny, kCount, kStackN>(s, r, eps, d2, valid, best_t, fc);
+}
+
 // Primary ray of pixel (px, py), src/scene_preprocessor.cpp:124-134.
 __device__ __forceinline__ RayF primary_ray(const CameraConsts &c, uint32_t px, uint32_t py) {
     const float x = (2 * (((float)px + 0.5f) * c.inv_w) - 1) * c.angle;

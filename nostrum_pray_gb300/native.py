@@ -25,6 +25,7 @@ CLI_PATH = os.path.join(_PKG, "_build", "Pray")
 PRAY_OK = 0
 TREE_MEDIAN, TREE_SAH = 0, 1
 PT_KAJIYA, PT_NEE, PT_DIFFUSE = 0, 1, 2
+TRAVERSAL_AUTO, TRAVERSAL_LANES, TRAVERSAL_PACKETS = -1, 0, 1
 SCHED_PIXEL, SCHED_WAVEFRONT, SCHED_AUTO = 0, 1, 2
 
 _vp = ctypes.c_void_p
@@ -71,7 +72,8 @@ EXPORTED = [
     "pray_last_error", "pray_api_version", "pray_tree_options_default", "pray_host_tree_build",
     "pray_host_tree_destroy", "pray_host_tree_stats", "pray_host_tree_dump", "pray_host_tree_precompute",
     "pray_host_tree_device_layout",
-    "pray_camera", "pray_scene_create", "pray_scene_destroy", "pray_scene_stats", "pray_trace_closest",
+    "pray_camera", "pray_scene_create", "pray_scene_destroy", "pray_scene_stats", "pray_scene_set_traversal",
+    "pray_scene_traversal", "pray_trace_closest",
     "pray_render_rt", "pray_render_rt_host", "pray_render_rt_counts", "pray_render_pt", "pray_render_pt_host",
     "pray_accumulate_pt", "pray_relmse", "pray_render_pt_noalloc",
     "pray_batch_create", "pray_batch_destroy", "pray_batch_set_config", "pray_batch_tune", "pray_batch_render",
@@ -101,6 +103,8 @@ def lib():
         L.pray_scene_create.argtypes = [_vp, _vp, _vp, _u64, ctypes.POINTER(TreeOptions), _i32, ctypes.POINTER(_vp)]
         L.pray_scene_destroy.argtypes = [_vp]
         L.pray_scene_stats.argtypes = [_vp, _vp]
+        L.pray_scene_set_traversal.argtypes = [_vp, _i32]
+        L.pray_scene_traversal.argtypes = [_vp, ctypes.POINTER(_i32)]
         L.pray_trace_closest.argtypes = [_vp, _vp, _u64, _f32, _vp, _vp, _vp]
         L.pray_render_rt.argtypes = [_vp, ctypes.POINTER(RtParams), _vp, _vp, _vp, _vp, _vp]
         L.pray_render_rt_host.argtypes = [_vp, ctypes.POINTER(RtParams), _vp, _vp]
@@ -270,6 +274,15 @@ class Scene:
         out = np.zeros(8, np.uint64)
         check(lib().pray_scene_stats(self._h, out.ctypes.data))
         return out
+
+    def set_traversal(self, traversal: int) -> None:
+        """TRAVERSAL_AUTO, TRAVERSAL_LANES or TRAVERSAL_PACKETS (ray-traced frames)."""
+        check(lib().pray_scene_set_traversal(self._h, traversal))
+
+    def traversal(self) -> int:
+        out = _i32(0)
+        check(lib().pray_scene_traversal(self._h, ctypes.byref(out)))
+        return int(out.value)
 
     # -- device-pointer entry points (torch CUDA tensors) --------------------
     def trace_closest(self, rays, det_eps: float, ids, ts, stream=None) -> None:

@@ -48,8 +48,9 @@ def trace(sc, rays, eps):
     return ids.cpu().numpy(), ts.cpu().numpy()
 
 
-def check_frame(oracle, mesh, setup):
+def check_frame(oracle, mesh, setup, traversal=native.TRAVERSAL_AUTO):
     sc = native.Scene.from_setup(mesh, setup)
+    sc.set_traversal(traversal)
     img, ids, ts, cnt = render(sc, setup)
     orc = oracle.OracleScene.from_setup(mesh, setup)
     want_img, want_sh = orc.render_rt(setup)
@@ -71,6 +72,36 @@ def check_frame(oracle, mesh, setup):
 @pytest.mark.parametrize("seed", [0, 1, 2])
 def test_soup_frame(oracle, seed):
     check_frame(oracle, scenes.soup(10_000, seed), scenes.soup_setup())
+
+
+@pytest.mark.parametrize("traversal", [native.TRAVERSAL_LANES, native.TRAVERSAL_PACKETS])
+@pytest.mark.parametrize("scene", ["soup", "sphere", "sah_soup"])
+def test_frame_traversals(oracle, traversal, scene):
+    """Both traversals of the ray-traced frame (per lane, and the warp packet
+    over a pixel tile) give the oracle's frame: hit ids, distances, image."""
+    if scene == "soup":
+        m, st = scenes.soup(10_000, 3), scenes.soup_setup(256, 192)
+    elif scene == "sphere":
+        m, st = scenes.icosphere(6), scenes.icosphere_setup(320, 240)
+    else:
+        m, st = scenes.soup(10_000, 4), scenes.soup_setup(320, 240)
+        st.tree, st.leaf_size, st.max_depth, st.sah_ct = "sah", 32, 20, 1.0
+    check_frame(oracle, m, st, traversal)
+
+
+def test_traversal_choice():
+    """AUTO picks one of the two traversals on the first frame and keeps it;
+    an explicit choice is kept as given."""
+    m, st = scenes.soup(2_000, 1), scenes.soup_setup(64, 64)
+    sc = native.Scene.from_setup(m, st)
+    assert sc.traversal() == native.TRAVERSAL_AUTO
+    sc.render_rt_host(st)
+    assert sc.traversal() in (native.TRAVERSAL_LANES, native.TRAVERSAL_PACKETS)
+    sc.set_traversal(native.TRAVERSAL_PACKETS)
+    sc.render_rt_host(st)
+    assert sc.traversal() == native.TRAVERSAL_PACKETS
+    with pytest.raises(native.PrayError):
+        sc.set_traversal(5)
 
 
 def test_soup_sah_default_constants(oracle):
