@@ -324,10 +324,10 @@ def run_ours(args):
                                     "triangle_fetches": tris, "shaded_hits": hits},
                          "dram_gbs": round(traffic / mean_s / 1e9, 1) if traffic else None,
                          "dram_frac": round(traffic / mean_s / 1e9 / peak, 4) if traffic else None,
-                         "note": ("the algorithmic node and triangle fetches are served mostly by L1 (93 % sector "
-                                  "hits) and L2 (74 %, ncu on this workload): the frame's working set reaches DRAM "
-                                  "once per launch (traffic), so frac exceeds 1; the kernel is bound by "
-                                  "instruction issue") if traffic else
+                         "note": ("the algorithmic node and triangle fetches (counted per ray) are served by "
+                                  "warp-wide broadcast loads from L1 (82 % sector hits) and L2 (81 %, ncu on this "
+                                  "workload): the frame's working set reaches DRAM once per launch (traffic), so "
+                                  "frac exceeds 1; the kernel is bound by instruction issue") if traffic else
                                  "scene L2-resident; no ncu traffic figure committed for this workload"},
             "wall_s_timed_loop": round(wall, 4), "clocks": clocks, "cpu_baseline": cpu}
     print(json.dumps(line), flush=True)

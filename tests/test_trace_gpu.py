@@ -75,17 +75,22 @@ def test_soup_frame(oracle, seed):
 
 
 @pytest.mark.parametrize("traversal", [native.TRAVERSAL_LANES, native.TRAVERSAL_PACKETS])
-@pytest.mark.parametrize("scene", ["soup", "sphere", "sah_soup"])
+@pytest.mark.parametrize("scene", ["soup", "sphere", "sah_soup", "far_camera"])
 def test_frame_traversals(oracle, traversal, scene):
     """Both traversals of the ray-traced frame (per lane, and the warp packet
-    over a pixel tile) give the oracle's frame: hit ids, distances, image."""
+    over a pixel tile) give the oracle's frame: hit ids, distances, image.
+    The distant camera's rays take the exact node copy, which packet warps
+    leave to the per-lane walk."""
     if scene == "soup":
         m, st = scenes.soup(10_000, 3), scenes.soup_setup(256, 192)
     elif scene == "sphere":
         m, st = scenes.icosphere(6), scenes.icosphere_setup(320, 240)
-    else:
+    elif scene == "sah_soup":
         m, st = scenes.soup(10_000, 4), scenes.soup_setup(320, 240)
         st.tree, st.leaf_size, st.max_depth, st.sah_ct = "sah", 32, 20, 1.0
+    else:
+        m, st = scenes.soup(10_000, 5), scenes.soup_setup(160, 120)
+        st.cam_pos, st.fov = (0.5, 0.5, -30.0), 3
     check_frame(oracle, m, st, traversal)
 
 
