@@ -168,13 +168,15 @@ pray_status pray_trace_closest(pray_scene *s, const float *rays_dev, uint64_t n,
 
 /* Traversal of a scene's ray-traced frames: each lane walks its own ray
  * (LANES), or the warp walks its pixel tile's rays as one packet with a
- * mask of the lanes whose own box tests passed (PACKETS); both return the
- * same hits. AUTO (the default) times both on the scene's first ray-traced
- * frame and keeps the faster. */
+ * mask of the lanes whose own box tests passed, for the primary and the
+ * occlusion rays (PACKETS) or for the primary rays only (PRIMARY_PACKETS);
+ * all return the same hits. AUTO (the default) times the three on the
+ * scene's first ray-traced frame and keeps the fastest. */
 typedef enum {
     PRAY_TRAVERSAL_AUTO = -1,
     PRAY_TRAVERSAL_LANES = 0,
-    PRAY_TRAVERSAL_PACKETS = 1
+    PRAY_TRAVERSAL_PACKETS = 1,
+    PRAY_TRAVERSAL_PRIMARY_PACKETS = 2
 } pray_traversal;
 pray_status pray_scene_set_traversal(pray_scene *s, int32_t traversal);
 /* The traversal in use (PRAY_TRAVERSAL_AUTO until the first frame chose). */
@@ -185,7 +187,7 @@ pray_status pray_scene_traversal(const pray_scene *s, int32_t *traversal);
  * may be NULL) receive the primary hits. counters_dev (may be NULL) is
  * incremented by [primary rays, occlusion rays]. Under PRAY_TRAVERSAL_AUTO
  * the scene's first ray-traced frame (this call, pray_render_rt_host or
- * pray_render_rt_counts) renders the frame five times to time the two
+ * pray_render_rt_counts) renders the frame seven times to time the three
  * traversals, and synchronises. */
 pray_status pray_render_rt(pray_scene *s, const pray_rt_params *p, uint8_t *rgb_dev, int32_t *ids_dev,
                            float *t_dev, unsigned long long *counters_dev, void *stream);

@@ -202,34 +202,41 @@ pray_status check_params(const pray_rt_params *p) {
 }
 
 // A ray-traced frame with the scene's traversal. The first frame of a scene
-// renders with the per-lane and with the warp-packet traversal, twice each,
-// times the second of each pair and keeps the faster for the scene (the
-// frames are identical; coherent surfaces favour packets, depth-complex
-// triangle soups the per-lane walk); it synchronises `stream`.
+// renders with each traversal (per lane, packets, packets for the primary
+// rays only) twice, times the second of each pair and keeps the fastest for
+// the scene (the frames are identical; coherent surfaces favour packets,
+// occlusion rays from the scattered hits of a triangle soup the per-lane
+// walk); it synchronises `stream`.
 cudaError_t render_rt(pray_scene *s, RtLaunch L, cudaStream_t stream) {
     if (s->rt_packets.load() < 0) {
+        constexpr int kModes = 3;
+        const int modes[kModes] = {PRAY_TRAVERSAL_LANES, PRAY_TRAVERSAL_PACKETS, PRAY_TRAVERSAL_PRIMARY_PACKETS};
         RtLaunch C = L;
         C.counters = nullptr;
         C.count_fetches = 0;
-        cudaEvent_t ev[4] = {};
+        cudaEvent_t ev[2 * kModes] = {};
         cudaError_t e = cudaSuccess;
         for (cudaEvent_t &x : ev)
             if (e == cudaSuccess) e = cudaEventCreate(&x);
         for (int rep = 0; rep < 2 && e == cudaSuccess; rep++)
-            for (int m = 0; m < 2 && e == cudaSuccess; m++) {
-                C.packets = m;
+            for (int m = 0; m < kModes && e == cudaSuccess; m++) {
+                C.packets = modes[m];
                 if (rep == 1) e = cudaEventRecord(ev[2 * m], stream);
                 if (e == cudaSuccess) e = launch_render_rt(s->view(), C, stream);
                 if (rep == 1 && e == cudaSuccess) e = cudaEventRecord(ev[2 * m + 1], stream);
             }
-        float ms[2] = {0.f, 0.f};
-        if (e == cudaSuccess) e = cudaEventSynchronize(ev[3]);
-        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[0], ev[0], ev[1]);
-        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[1], ev[2], ev[3]);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev[2 * kModes - 1]);
+        int best = 0;
+        float best_ms = 0.f;
+        for (int m = 0; m < kModes && e == cudaSuccess; m++) {
+            float ms = 0.f;
+            e = cudaEventElapsedTime(&ms, ev[2 * m], ev[2 * m + 1]);
+            if (m == 0 || ms < best_ms) best = m, best_ms = ms;
+        }
         for (cudaEvent_t x : ev)
             if (x) cudaEventDestroy(x);
         if (e != cudaSuccess) return e;
-        s->rt_packets.store(ms[1] < ms[0] ? 1 : 0);
+        s->rt_packets.store(modes[best]);
     }
     L.packets = s->rt_packets.load();
     return launch_render_rt(s->view(), L, stream);
@@ -590,8 +597,9 @@ pray_status pray_scene_destroy(pray_scene *s) {
 
 pray_status pray_scene_set_traversal(pray_scene *s, int32_t traversal) {
     if (!s) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (traversal < PRAY_TRAVERSAL_AUTO || traversal > PRAY_TRAVERSAL_PACKETS)
-        return set_error(PRAY_ERR_INVALID_ARGUMENT, "traversal must be PRAY_TRAVERSAL_AUTO, _LANES or _PACKETS");
+    if (traversal < PRAY_TRAVERSAL_AUTO || traversal > PRAY_TRAVERSAL_PRIMARY_PACKETS)
+        return set_error(PRAY_ERR_INVALID_ARGUMENT,
+                         "traversal must be PRAY_TRAVERSAL_AUTO, _LANES, _PACKETS or _PRIMARY_PACKETS");
     s->rt_packets.store(traversal);
     return PRAY_OK;
 }

@@ -3,6 +3,7 @@
 // light, quantisation). Traversal and intersection: traverse.cuh.
 #include <cfloat>
 #include <cstdint>
+#include <type_traits>
 
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -42,8 +43,9 @@ __global__ void __launch_bounds__(128) k_trace_closest(DevScene s, const float *
 // the quantisation of src/pray.cpp:576-588). Every lane of a warp runs the
 // same light loop so that the warp-collective traversals line up; a lane
 // whose colour saturated stops casting (the reference's early break).
-// kPacket: the warp traverses its tile's rays as a packet (traverse_coherent).
-template <bool kCount, int kStackN, bool kPacket>
+// kPrimPacket / kShadowPacket: the warp traverses its tile's primary /
+// occlusion rays as a packet (traverse_coherent).
+template <bool kCount, int kStackN, bool kPrimPacket, bool kShadowPacket>
 __global__ void __launch_bounds__(128, 8) k_render_rt(DevScene s, RtLaunch L) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t px, py;
@@ -56,8 +58,8 @@ __global__ void __launch_bounds__(128, 8) k_render_rt(DevScene s, RtLaunch L) {
     const RayF r = primary_ray(L.cam, active ? px : 0, active ? py : 0);
     float dist = FLT_MAX;
     const bool geo = active && s.n_refs > 0;
-    const int pos = kPacket ? traverse_coherent<false, kCount, kStackN>(s, r, L.eps, 0.f, geo, dist, stk, &fc)
-                            : traverse<false, kCount, kStackN>(s, r, L.eps, 0.f, geo, dist, &fc);
+    const int pos = kPrimPacket ? traverse_coherent<false, kCount, kStackN>(s, r, L.eps, 0.f, geo, dist, stk, &fc)
+                                : traverse<false, kCount, kStackN>(s, r, L.eps, 0.f, geo, dist, &fc);
     const bool hit = active && pos >= 0;
     float cr = L.bg[0], cg = L.bg[1], cb = L.bg[2];
     int32_t id = -1;
@@ -88,8 +90,8 @@ __global__ void __launch_bounds__(128, 8) k_render_rt(DevScene s, RtLaunch L) {
         shadows += need ? 1u : 0u;
         float dummy;
         const bool occluded =
-            (kPacket ? traverse_coherent<true, kCount, kStackN>(s, sr, L.eps, d2, need, dummy, stk, &fc)
-                     : traverse<true, kCount, kStackN>(s, sr, L.eps, d2, need, dummy, &fc)) >= 0;
+            (kShadowPacket ? traverse_coherent<true, kCount, kStackN>(s, sr, L.eps, d2, need, dummy, stk, &fc)
+                           : traverse<true, kCount, kStackN>(s, sr, L.eps, d2, need, dummy, &fc)) >= 0;
         if (need && !occluded) {
             const float w = 1.0f / d2;
             cr = cr + ((alb.x * L.lights[l][3]) * lambert) * w;
@@ -186,13 +188,17 @@ cudaError_t launch_render_rt(const DevScene &s, const RtLaunch &L, cudaStream_t 
     // a 32-entry stack (half the per-thread local memory) when the hierarchy is shallow enough
     const bool small = s.depth < 32;
     auto go = [&](auto kernel) { kernel<<<grid, bs, 0, stream>>>(s, L); };
-    if (L.count_fetches) {
-        if (L.packets) small ? go(k_render_rt<true, 32, true>) : go(k_render_rt<true, kStack, true>);
-        else small ? go(k_render_rt<true, 32, false>) : go(k_render_rt<true, kStack, false>);
-    } else {
-        if (L.packets) small ? go(k_render_rt<false, 32, true>) : go(k_render_rt<false, kStack, true>);
-        else small ? go(k_render_rt<false, 32, false>) : go(k_render_rt<false, kStack, false>);
-    }
+    // L.packets: 0 per lane, 1 primary and occlusion rays as packets, 2
+    // primary rays only
+    auto pick = [&](auto count) {
+        constexpr bool kC = decltype(count)::value;
+        if (L.packets == 1) small ? go(k_render_rt<kC, 32, true, true>) : go(k_render_rt<kC, kStack, true, true>);
+        else if (L.packets == 2)
+            small ? go(k_render_rt<kC, 32, true, false>) : go(k_render_rt<kC, kStack, true, false>);
+        else small ? go(k_render_rt<kC, 32, false, false>) : go(k_render_rt<kC, kStack, false, false>);
+    };
+    if (L.count_fetches) pick(std::true_type{});
+    else pick(std::false_type{});
     return cudaGetLastError();
 }
 

@@ -27,7 +27,8 @@ struct RtLaunch {
     float *ts;                       // optional out: primary hit distance per pixel (FLT_MAX: miss)
     unsigned long long *counters;    // optional out (accumulated): [0] primary rays, [1] occlusion rays
     int count_fetches;               // also accumulate [2] node-pair fetches, [3] triangle fetches, [4] shaded hits
-    int packets;                     // warp-packet traversal (traverse_packet) for warps that can take it
+    int packets;                     // pray_traversal: warp packets (traverse_packet) for primary and occlusion
+                                     // rays (1), primary rays only (2), none (0)
 };
 
 constexpr int kMaxPtDepth = 64;  // bounce limit of the path tracer (per-thread albedo stack)

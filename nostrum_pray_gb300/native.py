@@ -25,7 +25,7 @@ CLI_PATH = os.path.join(_PKG, "_build", "Pray")
 PRAY_OK = 0
 TREE_MEDIAN, TREE_SAH = 0, 1
 PT_KAJIYA, PT_NEE, PT_DIFFUSE = 0, 1, 2
-TRAVERSAL_AUTO, TRAVERSAL_LANES, TRAVERSAL_PACKETS = -1, 0, 1
+TRAVERSAL_AUTO, TRAVERSAL_LANES, TRAVERSAL_PACKETS, TRAVERSAL_PRIMARY_PACKETS = -1, 0, 1, 2
 SCHED_PIXEL, SCHED_WAVEFRONT, SCHED_AUTO = 0, 1, 2
 
 _vp = ctypes.c_void_p
@@ -276,7 +276,7 @@ class Scene:
         return out
 
     def set_traversal(self, traversal: int) -> None:
-        """TRAVERSAL_AUTO, TRAVERSAL_LANES or TRAVERSAL_PACKETS (ray-traced frames)."""
+        """TRAVERSAL_AUTO, _LANES, _PACKETS or _PRIMARY_PACKETS (ray-traced frames)."""
         check(lib().pray_scene_set_traversal(self._h, traversal))
 
     def traversal(self) -> int:

@@ -74,13 +74,15 @@ def test_soup_frame(oracle, seed):
     check_frame(oracle, scenes.soup(10_000, seed), scenes.soup_setup())
 
 
-@pytest.mark.parametrize("traversal", [native.TRAVERSAL_LANES, native.TRAVERSAL_PACKETS])
+@pytest.mark.parametrize("traversal", [native.TRAVERSAL_LANES, native.TRAVERSAL_PACKETS,
+                                       native.TRAVERSAL_PRIMARY_PACKETS])
 @pytest.mark.parametrize("scene", ["soup", "sphere", "sah_soup", "far_camera"])
 def test_frame_traversals(oracle, traversal, scene):
-    """Both traversals of the ray-traced frame (per lane, and the warp packet
-    over a pixel tile) give the oracle's frame: hit ids, distances, image.
-    The distant camera's rays take the exact node copy, which packet warps
-    leave to the per-lane walk."""
+    """Each traversal of the ray-traced frame (per lane; warp packets over a
+    pixel tile for the primary and occlusion rays, or for the primary rays
+    only) gives the oracle's frame: hit ids, distances, image. The distant
+    camera's rays take the exact node copy, which packet warps leave to the
+    per-lane walk."""
     if scene == "soup":
         m, st = scenes.soup(10_000, 3), scenes.soup_setup(256, 192)
     elif scene == "sphere":
@@ -95,13 +97,13 @@ def test_frame_traversals(oracle, traversal, scene):
 
 
 def test_traversal_choice():
-    """AUTO picks one of the two traversals on the first frame and keeps it;
-    an explicit choice is kept as given."""
+    """AUTO picks one of the traversals on the first frame and keeps it; an
+    explicit choice is kept as given."""
     m, st = scenes.soup(2_000, 1), scenes.soup_setup(64, 64)
     sc = native.Scene.from_setup(m, st)
     assert sc.traversal() == native.TRAVERSAL_AUTO
     sc.render_rt_host(st)
-    assert sc.traversal() in (native.TRAVERSAL_LANES, native.TRAVERSAL_PACKETS)
+    assert sc.traversal() in (native.TRAVERSAL_LANES, native.TRAVERSAL_PACKETS, native.TRAVERSAL_PRIMARY_PACKETS)
     sc.set_traversal(native.TRAVERSAL_PACKETS)
     sc.render_rt_host(st)
     assert sc.traversal() == native.TRAVERSAL_PACKETS
