@@ -306,9 +306,11 @@ def run_ours(args):
         v, cores, sample = cpu_baseline(mesh, setup, args.cpu_seconds)
         cpu = {"value": round(v, 4), "unit": "Mrays/s", "cores": cores, "kind": "port", "sample": sample}
     cfg = dict(cfg)
+    traversal = {native.TRAVERSAL_LANES: "per lane", native.TRAVERSAL_PACKETS: "warp packets",
+                 native.TRAVERSAL_PRIMARY_PACKETS: "warp packets for primary rays"}.get(sc.traversal(), "auto")
     cfg.update({"parallelism": f"replicas x{world}", "l2": "flushed between steps (256 MB write)",
                 "tree_build_s": round(build_s, 2), "rays_per_frame": rays_per_frame,
-                "leaf_refine": args.leaf_refine})
+                "leaf_refine": args.leaf_refine, "traversal": f"{traversal} (timed on the first frame)"})
     line = {"metric": "Mrays/s", "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(kernel_ms_max / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
