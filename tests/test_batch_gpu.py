@@ -18,13 +18,13 @@ def _cuda():
     native.lib()
 
 
-def small_batch():
+def small_batch(modes=(native.PT_KAJIYA,)):
     items = scenes.batch_workload(n=5, seed=3, median=3_000, lo=500, hi=20_000, spp=2, depth=4,
                                   resolutions=(24, 40, 56))
     scs, params, outs = [], [], []
     for i, (mesh, st) in enumerate(items):
         scs.append(native.Scene.from_setup(mesh, st))
-        params.append(native.pt_params(st, seed=100 + i, mode=native.PT_KAJIYA))
+        params.append(native.pt_params(st, seed=100 + i, mode=modes[i % len(modes)]))
         outs.append((torch.zeros((st.height, st.width, 3), dtype=torch.uint8, device="cuda"),
                      torch.zeros((st.height, st.width, 3), dtype=torch.float32, device="cuda")))
     return items, scs, params, outs
@@ -35,8 +35,12 @@ def alone(sc, p):
     return img, rad
 
 
-def test_batch_equals_single_scene_frames():
-    items, scs, params, outs = small_batch()
+@pytest.mark.parametrize("modes", [(native.PT_KAJIYA,), (native.PT_KAJIYA, native.PT_NEE)],
+                         ids=["kajiya", "mixed"])
+def test_batch_equals_single_scene_frames(modes):
+    """All-Kajiya batches run the per-lane state machine, batches with
+    next-event scenes the bounce-by-bounce loop; both equal single frames."""
+    items, scs, params, outs = small_batch(modes)
     b = native.Batch(scs, params, outs)
     cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
     want = [alone(sc, p) for sc, p in zip(scs, params)]
