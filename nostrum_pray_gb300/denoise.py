@@ -222,10 +222,16 @@ def denoised_eval(cfg: DenoiseConfig, den, sc, ref, room_seed: int, torch):
     p = _params(cfg, st, cfg.spp_in, seed=room_seed * 7 + 5)
     p2 = _params(cfg, st, cfg.spp_in, seed=room_seed * 7 + 6)
     pf = _params(cfg, st, 1, seed=0)
+    side = torch.cuda.Stream()
 
     def run():
+        # the first-hit features do not depend on the path-traced radiance:
+        # they render on a second stream beside it
+        main = torch.cuda.current_stream()
+        side.wait_stream(main)
+        sc.render_features(pf, feat[0], stream=side)
         sc.render_pt(p, None, rad[0])
-        sc.render_features(pf, feat[0])
+        main.wait_stream(side)
         den.denoise(rad, feat, out)
 
     run()
