@@ -338,7 +338,8 @@ __device__ __forceinline__ void pt_lanes(const DevScene &s, const PtLaunch &L, S
                 start_sample();
             }
         }
-        if (!__any_sync(kFull, job)) break;
+        // (a source may hand out slots outside the image: go on until it is drained)
+        if (!__any_sync(kFull, job) && src.drained()) break;
         trav_round<kClosest, false>(s, r, L.eps, 0.f, T, S, nullptr);
         if (job && !T.active()) {
             segments++;
