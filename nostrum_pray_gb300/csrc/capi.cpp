@@ -119,6 +119,7 @@ struct pray_scene {
     uint8_t *d_rgb = nullptr;
     uint64_t rgb_cap = 0;
     unsigned long long *d_counters = nullptr;
+    unsigned long long *d_pt_next = nullptr;  // work counter of the per-pixel path tracer
 
     DevScene view() const {
         DevScene v;
@@ -147,6 +148,8 @@ struct pray_scene {
         cudaFree(d_emit);
         cudaFree(d_emit_cdf);
         cudaFree(d_wf);
+        cudaFree(d_pt_next);
+        d_pt_next = nullptr;
         if (wf_exec) cudaGraphExecDestroy(wf_exec);
         if (wf_stream) cudaStreamDestroy(wf_stream);
         if (wf_ev_in) cudaEventDestroy(wf_ev_in);
@@ -325,23 +328,35 @@ pray_status run_pt(pray_scene *s, const PtLaunch &L, int scheduler, uint32_t wav
                      (uint64_t)L.cam.width * L.cam.height * L.num_samples >= kAutoWavefrontPaths)
                         ? PRAY_SCHED_WAVEFRONT
                         : PRAY_SCHED_PIXEL;
+    // both schedulers run on the scene's private stream (their scratch and
+    // work counters are the scene's), ordered after the caller's work
+    if (!s->wf_stream) {
+        if ((e = cudaStreamCreateWithFlags(&s->wf_stream, cudaStreamNonBlocking)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&s->wf_ev_in, cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&s->wf_ev_out, cudaEventDisableTiming)) != cudaSuccess)
+            return cuda_error(e, "path-tracer stream set-up");
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    }
     if (scheduler == PRAY_SCHED_PIXEL) {
-        e = launch_render_pt(s->view(), L, stream);
-        return e == cudaSuccess ? PRAY_OK : cuda_error(e, "render_pt launch");
+        if (!s->d_pt_next && (e = cudaMalloc(&s->d_pt_next, sizeof(unsigned long long))) != cudaSuccess)
+            return cuda_error(e, "cudaMalloc (pixel counter)");
+        PtLaunch P = L;
+        P.next_pixel = s->d_pt_next;
+        if ((e = cudaEventRecord(s->wf_ev_in, stream)) != cudaSuccess ||
+            (e = cudaStreamWaitEvent(s->wf_stream, s->wf_ev_in, 0)) != cudaSuccess ||
+            (e = cudaMemsetAsync(s->d_pt_next, 0, sizeof(unsigned long long), s->wf_stream)) != cudaSuccess ||
+            (e = launch_render_pt(s->view(), P, s->sm_count, s->wf_stream)) != cudaSuccess ||
+            (e = cudaEventRecord(s->wf_ev_out, s->wf_stream)) != cudaSuccess ||
+            (e = cudaStreamWaitEvent(stream, s->wf_ev_out, 0)) != cudaSuccess)
+            return cuda_error(e, "render_pt launch");
+        return PRAY_OK;
     }
     const uint64_t P = (uint64_t)L.cam.width * L.cam.height;
     const uint64_t max_paths = wavefront_paths ? wavefront_paths : kWavefrontMaxPaths;
     const uint64_t cap = std::max<uint64_t>(P, std::min<uint64_t>(P * L.num_samples, max_paths));
     if (cap >= (1ull << 32)) return set_error(PRAY_ERR_UNSUPPORTED, "frame too large for the wavefront scheduler");
-    if (!s->wf_stream) {
-        if ((e = cudaStreamCreateWithFlags(&s->wf_stream, cudaStreamNonBlocking)) != cudaSuccess ||
-            (e = cudaEventCreateWithFlags(&s->wf_ev_in, cudaEventDisableTiming)) != cudaSuccess ||
-            (e = cudaEventCreateWithFlags(&s->wf_ev_out, cudaEventDisableTiming)) != cudaSuccess)
-            return cuda_error(e, "wavefront stream set-up");
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, dev);
-    }
     if (s->wf_capacity < cap || s->wf_pixels < P) {
         const uint64_t ncap = std::max(cap, s->wf_capacity), npx = std::max(P, s->wf_pixels);
         const uint64_t bytes = wavefront_scratch_bytes(ncap, npx);

@@ -53,45 +53,98 @@ __device__ __forceinline__ uint32_t pick_emitter(const DevScene &s, float u) {
     return lo;
 }
 
-// Modes 0 and 1 bounce by bounce: all lanes of a warp call pt_pixel_sync
-// together and run each bounce's extension rays, then its next-event
-// occlusion rays, as two warp-collective traversals. Each lane works through
-// its own pixel's samples in order, and starts its next sample as soon as its
-// current path ends (path regeneration) instead of waiting for the warp's
-// longest path; the warp loops while any lane still has a path. The per-pixel
+// Pixels a lane takes one after another: a warp-collective source. All lanes
+// call take() together; a lane that asks (want) may receive a pixel.
+// OnePixel hands each lane one fixed pixel.
+struct OnePixel {
+    bool active;
+    uint32_t px, py;
+    bool given;
+    __device__ __forceinline__ bool drained() const { return given; }
+    __device__ __forceinline__ bool take(bool want, uint32_t &x, uint32_t &y) {
+        const bool got = want && !given && active;
+        given = true;
+        x = px, y = py;
+        return got;
+    }
+};
+
+// Modes 0 and 1 bounce by bounce: all lanes of a warp call pt_sync together
+// and run each bounce's extension rays, then its next-event occlusion rays,
+// as two warp-collective traversals. Each lane works through its pixel's
+// samples in order and starts its next sample as soon as its current path
+// ends (path regeneration); a lane whose pixel is done takes the next one
+// from `src`, so it does not wait for the warp's longest path. The per-pixel
 // sums still add the samples in sample order, so the result is unchanged.
-// The per-pixel kernel runs it for modes 0 and 1, the batch kernel for mode 1
-// (next-event occlusion rays, all aimed at the emitters, keep the warp more
-// coherent traced together than mixed with bounce rays).
-template <int kStackN>
-__device__ __forceinline__ void pt_pixel_sync(const DevScene &s, const PtLaunch &L, bool active, uint32_t px,
-                                         uint32_t py, uint32_t &segments) {
+// pixels counts the pixels a lane finished. The per-pixel kernel runs it for
+// modes 0 and 1, the batch kernel for mode 1 (next-event occlusion rays, all
+// aimed at the emitters, keep the warp more coherent traced together than
+// mixed with bounce rays).
+template <int kStackN, class Src>
+__device__ __forceinline__ void pt_sync(const DevScene &s, const PtLaunch &L, Src &src, uint32_t &segments,
+                                        uint32_t &pixels) {
     constexpr unsigned kFull = 0xFFFFFFFFu;
-    const uint64_t pixel = active ? (uint64_t)py * L.cam.width + px : 0;
-    const RayF prim = primary_ray(L.cam, active ? px : 0, active ? py : 0);
-    float sr = 0.f, sg = 0.f, sb = 0.f;
     float alb_r[kMaxPtDepth], alb_g[kMaxPtDepth], alb_b[kMaxPtDepth];
-    double ax = 0, ay = 0, az = 0;
-    if (active && L.sum64) ax = L.sum64[3 * pixel], ay = L.sum64[3 * pixel + 1], az = L.sum64[3 * pixel + 2];
     const bool any_geometry = s.n_refs > 0;
-    // the lane's current path
+    // the lane's pixel
+    bool have = false;
+    uint32_t px = 0, py = 0;
+    auto pixel = [&]() { return (uint64_t)py * L.cam.width + px; };
+    float sr = 0.f, sg = 0.f, sb = 0.f;
+    double ax = 0, ay = 0, az = 0;
+    // its current path
     uint32_t smp = 0;
     pray_pcg32 rng;
-    RayF r = prim;
+    RayF r{};
     float lr = 0.f, lg = 0.f, lb = 0.f;
     float tr = 1.f, tg = 1.f, tb = 1.f;
     uint32_t depth = 0;
     bool alive = false;
     auto start = [&]() {
-        rng = pray_pcg32_stream(L.seed, pixel, L.sample_offset + smp);
-        r = prim;
+        rng = pray_pcg32_stream(L.seed, pixel(), L.sample_offset + smp);
+        r = primary_ray(L.cam, px, py);
         lr = lg = lb = 0.f;
         tr = tg = tb = 1.f;
         depth = 0;
         alive = true;
     };
-    if (active && L.num_samples > 0) start();
-    while (__any_sync(kFull, alive)) {
+    auto finish_pixel = [&]() {
+        const uint64_t pix = pixel();
+        if (L.sum64) L.sum64[3 * pix] = ax, L.sum64[3 * pix + 1] = ay, L.sum64[3 * pix + 2] = az;
+        const float ns = (float)L.num_samples;
+        const float mr = sr / ns, mg = sg / ns, mb = sb / ns;
+        if (L.radiance) {
+            float *o = L.radiance + 3 * pix;
+            o[0] = mr, o[1] = mg, o[2] = mb;
+        }
+        if (L.rgb) {
+            uint8_t *o = L.rgb + 3 * pix;
+            o[0] = (uint8_t)quantise(smax(0.f, smin(1.f, mr)));
+            o[1] = (uint8_t)quantise(smax(0.f, smin(1.f, mg)));
+            o[2] = (uint8_t)quantise(smax(0.f, smin(1.f, mb)));
+        }
+        pixels++;
+        have = false;
+    };
+    while (true) {
+        const unsigned idle = __ballot_sync(kFull, !have);
+        if (idle && !src.drained()) {
+            uint32_t x, y;
+            if (src.take(!have, x, y)) {
+                have = true;
+                px = x, py = y;
+                smp = 0;
+                sr = sg = sb = 0.f;
+                ax = ay = az = 0;
+                if (L.sum64) {
+                    const uint64_t pix = pixel();
+                    ax = L.sum64[3 * pix], ay = L.sum64[3 * pix + 1], az = L.sum64[3 * pix + 2];
+                }
+                start();
+            }
+        }
+        // (a source may hand out slots outside the image: go on until it is drained)
+        if (!__any_sync(kFull, alive) && src.drained()) break;
         const bool was_alive = alive;
         float t;
         const int pos = traverse<false, false, kStackN>(s, r, L.eps, 0.f, alive && any_geometry, t);
@@ -188,40 +241,19 @@ __device__ __forceinline__ void pt_pixel_sync(const DevScene &s, const PtLaunch 
             sr = sr + lr, sg = sg + lg, sb = sb + lb;
             if (L.sum64) ax = ax + (double)lr, ay = ay + (double)lg, az = az + (double)lb;
             if (++smp < L.num_samples) start();
-        }
-    }
-    if (active) {
-        if (L.sum64) L.sum64[3 * pixel] = ax, L.sum64[3 * pixel + 1] = ay, L.sum64[3 * pixel + 2] = az;
-        const float ns = (float)L.num_samples;
-        const float mr = sr / ns, mg = sg / ns, mb = sb / ns;
-        if (L.radiance) {
-            float *o = L.radiance + 3 * pixel;
-            o[0] = mr, o[1] = mg, o[2] = mb;
-        }
-        if (L.rgb) {
-            uint8_t *o = L.rgb + 3 * pixel;
-            o[0] = (uint8_t)quantise(smax(0.f, smin(1.f, mr)));
-            o[1] = (uint8_t)quantise(smax(0.f, smin(1.f, mg)));
-            o[2] = (uint8_t)quantise(smax(0.f, smin(1.f, mb)));
+            else finish_pixel();
         }
     }
 }
 
-// Pixels a lane takes one after another: a warp-collective source. All lanes
-// call take() together; a lane that asks (want) may receive a pixel.
-// OnePixel hands each lane one fixed pixel.
-struct OnePixel {
-    bool active;
-    uint32_t px, py;
-    bool given;
-    __device__ __forceinline__ bool drained() const { return given; }
-    __device__ __forceinline__ bool take(bool want, uint32_t &x, uint32_t &y) {
-        const bool got = want && !given && active;
-        given = true;
-        x = px, y = py;
-        return got;
-    }
-};
+// One fixed pixel per lane (active lanes).
+template <int kStackN>
+__device__ __forceinline__ void pt_pixel_sync(const DevScene &s, const PtLaunch &L, bool active, uint32_t px,
+                                         uint32_t py, uint32_t &segments) {
+    OnePixel src{active, px, py, false};
+    uint32_t pixels = 0;
+    pt_sync<kStackN>(s, L, src, segments, pixels);
+}
 
 // Mode 0 as a per-lane state machine (the batch kernel's: 355 against 296
 // Msamples/s on the 64-scene batch). All lanes of a warp call pt_lanes

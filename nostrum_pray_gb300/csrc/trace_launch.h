@@ -46,9 +46,12 @@ struct PtLaunch {
     float *radiance;                 // optional out: height x width x 3 mean radiance
     double *sum64;                   // optional in/out: height x width x 3 FP64 sums, samples added in order
     unsigned long long *counters;    // optional out (accumulated): [0] paths, [1] ray segments
+    unsigned long long *next_pixel;  // per-pixel kernel: work counter of the frame (zero at launch)
 };
 
-cudaError_t launch_render_pt(const DevScene &s, const PtLaunch &L, cudaStream_t stream);
+// Per-pixel kernel on `sm_count` SMs; mode 1 needs L.next_pixel (zeroed on
+// the stream before the launch; one frame at a time per counter).
+cudaError_t launch_render_pt(const DevScene &s, const PtLaunch &L, int sm_count, cudaStream_t stream);
 
 // Wavefront path tracer (wavefront.cu): path pool and queues in `scratch`.
 struct WavefrontScratch {
