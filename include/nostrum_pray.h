@@ -207,7 +207,9 @@ pray_status pray_render_rt_counts(pray_scene *s, const pray_rt_params *p, uint64
  * memory: rgb_dev as for pray_render_rt (may be NULL when radiance_dev is
  * given); radiance_dev (may be NULL) receives
  * the per-pixel mean radiance (height x width x 3 floats) before clamping;
- * counters_dev (may be NULL) is incremented by [paths, ray segments]. */
+ * counters_dev (may be NULL) is incremented by [paths, ray segments]. The
+ * frame runs on the scene's own stream, after `stream`'s earlier work and
+ * before its later work; frames of one scene run one after another. */
 pray_status pray_render_pt(pray_scene *s, const pray_pt_params *p, uint8_t *rgb_dev, float *radiance_dev,
                            unsigned long long *counters_dev, void *stream);
 
