@@ -48,6 +48,15 @@ def test_nee_room(oracle):
     compare(oracle, m, st, spp=8, depth=8, seed=4, mode=native.PT_NEE, rr=3)
 
 
+def test_nee_ragged_frame(oracle):
+    """A frame whose size is no multiple of the 8 x 4 warp tile: the per-pixel
+    kernel's lanes take pixels from a frame counter, including the slots of
+    ragged tiles outside the image."""
+    m = scenes.room(grid=5)
+    st = scenes.room_setup(37, 23)
+    compare(oracle, m, st, spp=3, depth=6, seed=11, mode=native.PT_NEE, rr=2)
+
+
 def test_kajiya_background_and_median_tree(oracle):
     m = scenes.soup(2_000, 1)
     m.emit[::7] = 1
