@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--dn-train-res", type=int, default=512, help="denoise: training image size")
     ap.add_argument("--dn-cuda-cores", action="store_true", help="denoise-infer: CUDA-core convolutions")
     ap.add_argument("--dn-spp-in", type=int, default=4, help="denoise: samples per pixel of the noisy input")
+    ap.add_argument("--dn-depth-in", type=int, default=0,
+                    help="denoise: path depth of the noisy input (0: the full depth of the references)")
     ap.add_argument("--dn-ref-spp", type=int, default=1024, help="denoise: training target samples per pixel")
     ap.add_argument("--dn-eval-ref-spp", type=int, default=4096,
                     help="denoise: samples per pixel of the held-out rooms' references")
@@ -448,7 +450,7 @@ def run_denoise(args):
     torch.cuda.set_device(0)
     cfg = D.DenoiseConfig(res=args.dn_res, train_res=args.dn_train_res, spp_ref=args.dn_ref_spp,
                           train_rooms=args.dn_train, eval_rooms=args.dn_eval, steps=args.dn_steps,
-                          spp_in=args.dn_spp_in)
+                          spp_in=args.dn_spp_in, depth_in=args.dn_depth_in)
     t0 = time.perf_counter()
     train_seeds = list(range(cfg.seed, cfg.seed + cfg.train_rooms))
     eval_seeds = list(range(cfg.seed + 100_000, cfg.seed + 100_000 + cfg.eval_rooms))
@@ -475,7 +477,9 @@ def run_denoise(args):
     ok_d = sum(1 for r in rows if r["relmse_final"] <= cfg.target)
     line = {"metric": "time to relMSE<=0.01, denoised / plain", "value": round(float(np.mean(td) / np.mean(tp)), 4)
             if tp else None, "unit": "ratio", "n_gpus": 1, "higher_is_better": False, "dtype": "bf16",
-            "data": "synthetic", "config": {"workload": f"procedural rooms, evaluated at {cfg.res}x{cfg.res}, {cfg.spp_in} spp input,"
+            "data": "synthetic", "config": {"workload": f"procedural rooms, evaluated at {cfg.res}x{cfg.res}, {cfg.spp_in} spp input"
+                                                        f"{f' (paths cut at {cfg.depth_in} bounces)' if cfg.depth_in else ''},"
+                                                        f" path depth {cfg.depth} (RR from {cfg.rr_depth}),"
                                                         f" {cfg.spp_ref} spp FP64 training targets,"
                                                         f" {eval_cfg.spp_ref} spp FP64 evaluation references, {cfg.train_rooms} train rooms"
                                                         f" at {cfg.train_res}^2 ({cfg.crop}^2 crops, batch {cfg.batch}),"

@@ -3,7 +3,8 @@ evaluation of the U-Net (pray_denoiser_* in include/nostrum_pray.h).
 
 Data: seeded procedural rooms (scenes.random_room), each rendered with the
 next-event-estimation path tracer at a few samples per pixel (the noisy
-input), with its first-hit features, and at many samples per pixel
+input; optionally with its paths cut at fewer bounces), with its first-hit
+features, and at many samples per pixel
 accumulated in FP64 (the reference). The denoiser divides radiance by the
 first-hit albedo (+0.05) before the network and multiplies it back after
 (pray_denoise). The network
@@ -38,6 +39,7 @@ class DenoiseConfig:
     spp_in: int = 4
     spp_ref: int = 1024
     depth: int = 8
+    depth_in: int = 0        # path depth of the noisy input (0: depth); references and plain renders use depth
     rr_depth: int = 3
     train_rooms: int = 96
     eval_rooms: int = 16
@@ -83,9 +85,17 @@ def _setup(cfg: DenoiseConfig, res: Optional[int] = None):
     return scenes.room_setup(r, r, spp=cfg.spp_in, max_depth=cfg.depth)
 
 
-def _params(cfg, st, spp, seed, offset=0):
-    return native.pt_params(st, spp=spp, max_depth=cfg.depth, seed=seed, mode=native.PT_NEE,
-                            rr_depth=cfg.rr_depth, scheduler=native.SCHED_AUTO, sample_offset=offset)
+def _params(cfg, st, spp, seed, offset=0, depth=None):
+    return native.pt_params(st, spp=spp, max_depth=cfg.depth if depth is None else depth, seed=seed,
+                            mode=native.PT_NEE, rr_depth=cfg.rr_depth, scheduler=native.SCHED_AUTO,
+                            sample_offset=offset)
+
+
+def input_params(cfg, st, seed):
+    """The noisy input's render: spp_in samples per pixel, paths cut at
+    depth_in bounces when it is set (the network then also restores the light
+    of the longer paths, which the references and plain renders keep)."""
+    return _params(cfg, st, cfg.spp_in, seed, depth=cfg.depth_in or cfg.depth)
 
 
 def render_room(cfg: DenoiseConfig, room_seed: int, torch, res: Optional[int] = None):
@@ -95,7 +105,7 @@ def render_room(cfg: DenoiseConfig, room_seed: int, torch, res: Optional[int] = 
     h = w = st.width
     rad = torch.empty((h, w, 3), dtype=torch.float32, device="cuda")
     rgb = torch.empty((h, w, 3), dtype=torch.uint8, device="cuda")
-    sc.render_pt(_params(cfg, st, cfg.spp_in, seed=room_seed * 7 + 1), rgb, rad)
+    sc.render_pt(input_params(cfg, st, seed=room_seed * 7 + 1), rgb, rad)
     feat = torch.empty((h, w, 7), dtype=torch.float16, device="cuda")
     sc.render_features(_params(cfg, st, 1, seed=0), feat)
     ref = torch.zeros((h, w, 3), dtype=torch.float64, device="cuda")
@@ -219,8 +229,8 @@ def denoised_eval(cfg: DenoiseConfig, den, sc, ref, room_seed: int, torch):
     feat = torch.empty((1, h, w, 7), dtype=torch.float16, device="cuda")
     out = torch.empty((1, h, w, 3), dtype=torch.float32, device="cuda")
     out2 = torch.empty((1, h, w, 3), dtype=torch.float32, device="cuda")
-    p = _params(cfg, st, cfg.spp_in, seed=room_seed * 7 + 5)
-    p2 = _params(cfg, st, cfg.spp_in, seed=room_seed * 7 + 6)
+    p = input_params(cfg, st, seed=room_seed * 7 + 5)
+    p2 = input_params(cfg, st, seed=room_seed * 7 + 6)
     pf = _params(cfg, st, 1, seed=0)
     side = torch.cuda.Stream()
 

@@ -195,3 +195,16 @@ def test_plain_time_to_target_bisects():
     assert denoise.smallest_spp(curve, 0.001, measure) is None and not seen
     # the first count already meets it: bisect from zero
     assert denoise.smallest_spp(curve[2:], 0.04, measure) == (3, 0.1 / 3, 3e-3)
+
+
+def test_denoiser_input_depth():
+    """A cut input depth applies to the noisy input's render only: the
+    references and the plain renders keep the full path depth."""
+    from nostrum_pray_gb300 import denoise
+    cfg = denoise.DenoiseConfig(res=64, spp_in=1, depth_in=3)
+    st = denoise._setup(cfg)
+    p_in = denoise.input_params(cfg, st, seed=5)
+    assert (p_in.max_depth, p_in.num_samples, p_in.rr_depth) == (3, 1, cfg.rr_depth)
+    assert denoise._params(cfg, st, 16, seed=5).max_depth == cfg.depth == 8
+    full = denoise.DenoiseConfig(res=64, spp_in=4)
+    assert denoise.input_params(full, denoise._setup(full), seed=5).max_depth == 8
