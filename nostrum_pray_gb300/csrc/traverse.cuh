@@ -79,6 +79,26 @@ __device__ __forceinline__ bool slab(const float4 &lo, const float4 &hi, const R
     return slab(lo, hi, r, false, tn, tf);
 }
 
+// The slab test on the culling copy's padded boxes as one FMA per plane:
+// (p - o) * inv computed as p * inv + (-o * inv), with no = -o * inv rounded
+// once per ray (finite: the caller checks). Its error against the exact
+// plane distance is below 2^-23 (|p| + |o|) |inv| per axis, where the
+// padding of a culling box moves each plane by at least 2^-16 (|p| + scene
+// diagonal) and culling origins lie within 4 diagonals of the scene's
+// centre, so |o| < |p| + 5 diagonals: every plane distance keeps a margin of
+// about 2^6 times its error, on entry and exit, so no box that the exact
+// ray crosses (around any triangle it hits) fails the test or the pruning
+// bound.
+__device__ __forceinline__ bool slab_fma(const float4 &lo, const float4 &hi, const RayF &r, float nox, float noy,
+                                         float noz, float &tn, float &tf) {
+    const float t1x = fmaf(lo.x, r.ix, nox), t2x = fmaf(hi.x, r.ix, nox);
+    const float t1y = fmaf(lo.y, r.iy, noy), t2y = fmaf(hi.y, r.iy, noy);
+    const float t1z = fmaf(lo.z, r.iz, noz), t2z = fmaf(hi.z, r.iz, noz);
+    tn = fmaxf(fmaxf(fminf(t1x, t2x), fminf(t1y, t2y)), fmaxf(fminf(t1z, t2z), -FLT_MAX));
+    tf = fminf(fminf(fmaxf(t1x, t2x), fmaxf(t1y, t2y)), fminf(fmaxf(t1z, t2z), FLT_MAX));
+    return tn <= tf;
+}
+
 // One-sided Moeller-Trumbore, include/geometry.h:242-262, with the det
 // threshold as a parameter (the reference's EPSILON is 1e-4).
 __device__ __forceinline__ bool intersect_tri(const float4 &v0, const float4 &e1, const float4 &e2, const RayF &r,
@@ -317,14 +337,16 @@ __device__ __forceinline__ int traverse(const DevScene &s, const RayF &r, float 
 // of visits differs (the warp enters first the child that is nearer for most
 // of the lanes entering both), and a lane whose bound shrank after a node was
 // pushed still visits it (testing a popped node's box again measured slower:
-// 2,571 against 2,682 Mrays/s on the 1.31M sphere). Only for warps whose
-// valid lanes all use the culling copy.
+// 2,571 against 2,682 Mrays/s on the 1.31M sphere). Box tests run in FMA
+// form (slab_fma). Only for warps whose valid lanes all use the culling
+// copy.
 template <bool kAny, bool kCount, int kStackN>
 __device__ __forceinline__ int traverse_packet(const DevScene &s, const RayF &r, float eps, float d2, bool valid,
                                                float &best_t, uint32_t *stk, FetchCount *fc) {
     constexpr unsigned kFull = 0xFFFFFFFFu;
     const uint32_t lane = threadIdx.x & 31u;
     const GNode *nodes = s.nodes + s.n_nodes;
+    const float nox = -(r.ox * r.ix), noy = -(r.oy * r.iy), noz = -(r.oz * r.iz);
     float limit = kAny ? sqrtf(d2) * kPruneRel : FLT_MAX;
     const float back = -s.tol;
     best_t = FLT_MAX;
@@ -335,7 +357,7 @@ __device__ __forceinline__ int traverse_packet(const DevScene &s, const RayF &r,
     {
         const float4 lo = ldg4(nodes[0].lo), hi = ldg4(nodes[0].hi);
         float tn, tf;
-        mask = __ballot_sync(kFull, valid && slab(lo, hi, r, true, tn, tf));
+        mask = __ballot_sync(kFull, valid && slab_fma(lo, hi, r, nox, noy, noz, tn, tf));
         a = __float_as_uint(lo.w);
         b = __float_as_uint(hi.w);
     }
@@ -347,8 +369,8 @@ __device__ __forceinline__ int traverse_packet(const DevScene &s, const RayF &r,
             const float4 l0 = ldg4(c[0].lo), h0 = ldg4(c[0].hi), l1 = ldg4(c[1].lo), h1 = ldg4(c[1].hi);
             if (kCount && in) fc->pairs++;
             float tn0, tf0, tn1, tf1;
-            const bool v0 = in && slab(l0, h0, r, true, tn0, tf0) && tn0 <= limit && tf0 >= back;
-            const bool v1 = in && slab(l1, h1, r, true, tn1, tf1) && tn1 <= limit && tf1 >= back;
+            const bool v0 = in && slab_fma(l0, h0, r, nox, noy, noz, tn0, tf0) && tn0 <= limit && tf0 >= back;
+            const bool v1 = in && slab_fma(l1, h1, r, nox, noy, noz, tn1, tf1) && tn1 <= limit && tf1 >= back;
             const unsigned m0 = __ballot_sync(kFull, v0), m1 = __ballot_sync(kFull, v1);
             if (m0 && m1) {
                 const unsigned both = m0 & m1;
@@ -416,12 +438,15 @@ __device__ __forceinline__ int traverse_packet(const DevScene &s, const RayF &r,
     return best;
 }
 
-// traverse_packet where every valid lane of the warp uses the culling copy,
-// else traverse(); all lanes of the warp call it together.
+// traverse_packet where every valid lane of the warp uses the culling copy
+// (and has a finite o * inv on every axis), else traverse(); all lanes of
+// the warp call it together.
 template <bool kAny, bool kCount, int kStackN>
 __device__ __forceinline__ int traverse_coherent(const DevScene &s, const RayF &r, float eps, float d2, bool valid,
                                                  float &best_t, uint32_t *stk, FetchCount *fc = nullptr) {
-    const bool finite = isfinite(r.ix) && isfinite(r.iy) && isfinite(r.iz);
+    // the packet's FMA slab test also needs o * inv finite
+    const bool finite = isfinite(r.ix) && isfinite(r.iy) && isfinite(r.iz) && isfinite(r.ox * r.ix) &&
+                        isfinite(r.oy * r.iy) && isfinite(r.oz * r.iz);
     const float cx = r.ox - s.cull_c[0], cy = r.oy - s.cull_c[1], cz = r.oz - s.cull_c[2];
     const bool cull = finite && cx * cx + cy * cy + cz * cz <= s.cull_r2;
     if (__all_sync(0xFFFFFFFFu, !valid || cull))
