@@ -20,7 +20,8 @@ constexpr float kPadRel = 1.0f / 65536.0f;
 // its triangle by about u(R + D) / (sin a sin b), a the triangle's smallest
 // angle and b the ray's angle to its plane. The pad, 2^8 u D, keeps such hits
 // inside their boxes for sin a sin b down to 1/50 at the reach limit (1/170
-// for origins inside the scene).
+// for origins inside the scene). The warp-packet walk's FMA form of the slab
+// test (p * inv - o * inv) adds at most 1/25 of the pad.
 constexpr float kPadScene = 1.0f / 65536.0f;
 constexpr float kCullReach = 4.0f;
 // deepest node the flattened hierarchy may have (the kernels' traversal stack

@@ -82,13 +82,13 @@ __device__ __forceinline__ bool slab(const float4 &lo, const float4 &hi, const R
 // The slab test on the culling copy's padded boxes as one FMA per plane:
 // (p - o) * inv computed as p * inv + (-o * inv), with no = -o * inv rounded
 // once per ray (finite: the caller checks). Its error against the exact
-// plane distance is below 2^-23 (|p| + |o|) |inv| per axis, where the
-// padding of a culling box moves each plane by at least 2^-16 (|p| + scene
-// diagonal) and culling origins lie within 4 diagonals of the scene's
-// centre, so |o| < |p| + 5 diagonals: every plane distance keeps a margin of
-// about 2^6 times its error, on entry and exit, so no box that the exact
-// ray crosses (around any triangle it hits) fails the test or the pruning
-// bound.
+// plane distance is below 2^-24 (2 |o| + |p|) |inv| per axis. The padding
+// of a culling box moves each plane by at least 2^-16 (|p| + D) (D the
+// scene's diagonal) and culling origins lie within 4 D of the scene's
+// centre, so |o| < |p| + 4.5 D and the error is below 1/25 of the pad, on
+// entry and exit alike: the pad still holds the triangle hits it was sized
+// for (host/flatten.cpp), so no box that the exact ray crosses around a hit
+// fails the test or the pruning bound.
 __device__ __forceinline__ bool slab_fma(const float4 &lo, const float4 &hi, const RayF &r, float nox, float noy,
                                          float noz, float &tn, float &tf) {
     const float t1x = fmaf(lo.x, r.ix, nox), t2x = fmaf(hi.x, r.ix, nox);
