@@ -258,7 +258,6 @@ cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h
         Buf &cat = act_[idx];
         const Buf &low = act_[prev];
         const Buf &skip = act_[skip_idx[k]];
-        const size_t p = (size_t)n * (h >> l) * (w >> l);
         chk(dn::upsample_concat(low.x, skip.x, cat.x, n, h >> (l + 1), w >> (l + 1), low.c, skip.c, st));
         prev = idx++;
         chk(conv_fwd(conv++, act_[prev], act_[idx].x, nullptr, st));
