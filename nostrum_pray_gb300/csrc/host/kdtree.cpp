@@ -86,6 +86,42 @@ inline bool ev_less(const Ev &a, const Ev &b) {
     return (a.d < b.d) || (a.d == b.d && a.axis < b.axis) || (a.d == b.d && a.axis == b.axis && a.type < b.type);
 }
 
+// Sorts events by ev_less on up to `threads` threads: a power-of-two number
+// of chunks sorted concurrently, then merged pairwise. Events that compare
+// equal are interchangeable, so the tree does not depend on their order.
+void sort_events(std::vector<Ev> &ev, int threads) {
+    const size_t n = ev.size();
+    int parts = 1;
+    while (2 * parts <= threads && n / (2 * (size_t)parts) >= ((size_t)1 << 16)) parts *= 2;
+    if (parts == 1) {
+        std::sort(ev.begin(), ev.end(), ev_less);
+        return;
+    }
+    std::vector<size_t> cut(parts + 1);
+    for (int i = 0; i <= parts; i++) cut[i] = n * (size_t)i / (size_t)parts;
+    {
+        std::vector<std::thread> pool;
+        for (int i = 0; i < parts; i++)
+            pool.emplace_back([&, i] { std::sort(ev.begin() + cut[i], ev.begin() + cut[i + 1], ev_less); });
+        for (auto &t : pool) t.join();
+    }
+    std::vector<Ev> tmp(n);
+    std::vector<Ev> *src = &ev, *dst = &tmp;
+    for (int w = 1; w < parts; w *= 2) {
+        std::vector<std::thread> pool;
+        for (int i = 0; i < parts; i += 2 * w) {
+            const size_t a = cut[i], m = cut[i + w], b = cut[i + 2 * w];
+            pool.emplace_back([=] {
+                std::merge(src->begin() + a, src->begin() + m, src->begin() + m, src->begin() + b, dst->begin() + a,
+                           ev_less);
+            });
+        }
+        for (auto &t : pool) t.join();
+        std::swap(src, dst);
+    }
+    if (src != &ev) ev.swap(tmp);
+}
+
 enum : int8_t { kLeftOnly = -1, kBoth = 0, kRightOnly = 1 };
 
 struct SahBuilder {
@@ -322,7 +358,7 @@ BuiltTree build_tree(const std::vector<TriPre> &tris, const TreeOptions &opt) {
         std::vector<Ev> ev;
         ev.reserve(tris.size() * 6);
         for (uint32_t t : idx) sb.events_of(t, rb, ev);
-        std::sort(ev.begin(), ev.end(), ev_less);
+        sort_events(ev, threads);
         std::vector<int8_t> side(tris.size(), kBoth);
         root = sb.build(idx, rb, std::move(ev), 255, 0.f, 0, side);
     }
