@@ -82,6 +82,18 @@ def test_host_sah_tree_full_icosphere(golden):
     assert dump_hash(t.tree_dump()) == hashes["ico8_eps0"]["tree"]
 
 
+@pytest.mark.parametrize("threads", [1, 3, 16])
+def test_host_sah_tree_independent_of_threads(golden, threads):
+    """The parallel builder (subtrees and the root's event sort split over
+    threads) gives the reference's tree for any thread count."""
+    hashes, _ = golden
+    o = native.tree_options(scenes.icosphere_setup())
+    o.build_threads = threads
+    t = native.HostTree(scenes.icosphere(8), o)
+    assert [int(x) for x in t.tree_stats()] == hashes["ico8_eps0"]["stats"]
+    assert dump_hash(t.tree_dump()) == hashes["ico8_eps0"]["tree"]
+
+
 def test_host_precompute_matches_reference(golden):
     _, small = golden
     t = native.HostTree(scenes.soup(10_000, 0), native.tree_options(scenes.soup_setup()))
