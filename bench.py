@@ -165,31 +165,30 @@ def committed_traffic(kernel: str, workload_name: str):
     return None
 
 
-def cpu_baseline(mesh, setup, budget_s: float, threads=None):
-    """The oracle's restatement of the reference's tracer (full depth-first
-    traversal, scalar Moeller-Trumbore, OpenMP over rows) on a bounded sample of
-    central image rows. Returns (Mrays/s, cores, sample description)."""
+def cpu_frames(orc, setup, budget_s: float, min_frames: int = 1):
+    """Whole ray-traced frames of the oracle's restatement of the reference's
+    tracer (full depth-first traversal, scalar Moeller-Trumbore, OpenMP over
+    pixels on every host thread) until `budget_s` is spent. Returns (seconds,
+    rays, frames, threads OpenMP ran with)."""
+    from oracle import oracle as O
+    elapsed, rays, frames = 0.0, 0, 0
+    while frames < min_frames or elapsed < budget_s:
+        t0 = time.perf_counter()
+        _, nsh = orc.render_rt(setup, threads=O.default_threads())
+        elapsed += time.perf_counter() - t0
+        rays += setup.width * setup.height + nsh
+        frames += 1
+    return elapsed, rays, frames, O.last_threads()
+
+
+def cpu_baseline(mesh, setup, budget_s: float):
+    """The CPU port timed beside the GPU: whole frames of the same workload.
+    Returns (Mrays/s, threads, sample description)."""
     from oracle import oracle as O
     O.build()
     orc = O.OracleScene.from_setup(mesh, setup)
-    thr = threads or O.default_threads()
-    mid = setup.height // 2
-    rows, rays, elapsed = 0, 0, 0.0
-    chunk = 8
-    lo = hi = mid
-    while elapsed < budget_s and (lo > 0 or hi < setup.height):
-        a, b = max(0, lo - chunk // 2), min(setup.height, hi + chunk // 2)
-        for r0, r1 in ((a, lo), (hi, b)):
-            if r1 <= r0:
-                continue
-            t0 = time.perf_counter()
-            _, nsh = orc.render_rt(setup, rows=(r0, r1), threads=thr)
-            elapsed += time.perf_counter() - t0
-            rays += (r1 - r0) * setup.width + nsh
-            rows += r1 - r0
-        lo, hi = a, b
-    return rays / elapsed / 1e6, thr, f"{rows} central rows of {setup.height} ({rows * setup.width} pixels, " \
-                                      f"{rays} rays) in {elapsed:.1f} s"
+    elapsed, rays, frames, thr = cpu_frames(orc, setup, budget_s)
+    return rays / elapsed / 1e6, thr, f"{frames} whole frame(s) ({rays} rays) in {elapsed:.1f} s"
 
 
 def run_reference(args):
@@ -200,22 +199,15 @@ def run_reference(args):
     from oracle import oracle as O
     O.build()
     orc = O.OracleScene.from_setup(mesh, setup)
-    thr = O.default_threads()
-    rows = 24
-    r0 = setup.height // 2 - rows // 2
-    def step():
-        t0 = time.perf_counter()
-        _, nsh = orc.render_rt(setup, rows=(r0, r0 + rows), threads=thr)
-        return time.perf_counter() - t0, rows * setup.width + nsh
     for _ in range(args.warmup):
-        step()
-    total_t, total_r = 0.0, 0
+        cpu_frames(orc, setup, 0.0)
+    total_t, total_r, thr = 0.0, 0, 0
     for _ in range(args.steps):
-        t, r = step()
+        t, r, _, thr = cpu_frames(orc, setup, 0.0)
         total_t += t
         total_r += r
     v = total_r / total_t / 1e6
-    sample = f"each step: {rows} central rows x {setup.width} pixels with their occlusion rays"
+    sample = f"each step: one whole frame ({setup.width}x{setup.height} pixels with their occlusion rays)"
     line = {"impl": "reference", "metric": "Mrays/s", "value": round(v, 4), "unit": "Mrays/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1e3 * total_t / args.steps, 3), "higher_is_better": True, "scaling": "weak",
@@ -223,8 +215,9 @@ def run_reference(args):
             "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": thr, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(v, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "CPU restatement of the reference's scalar tracer (oracle/pray_oracle.cpp); the reference's "
-                    "own x86 AVX build does not run on this host"}
+            "note": "CPU restatement of the reference's scalar tracer (oracle/pray_oracle.cpp), OpenMP over pixels "
+                    "on every host thread; the reference's sources are not on this host, and its own build (x86 "
+                    "AVX) would not run here"}
     print(json.dumps(line), flush=True)
 
 
@@ -384,14 +377,14 @@ def run_pt(args):
         from oracle import oracle as O
         O.build()
         orc = O.OracleScene.from_setup(mesh, st)
-        thr = O.default_threads()
         row, rows, elapsed = st.height // 2, 0, 0.0
         while elapsed < args.cpu_seconds and row < st.height:
             t0 = time.perf_counter()
-            orc.render_pt(st, spp=spp, max_depth=8, seed=1, mode=native.PT_NEE, rr_depth=3, rows=(row, row + 1),
-                          threads=thr)
+            orc.render_pt(st, spp=spp, max_depth=8, seed=1, mode=native.PT_NEE, rr_depth=3, rows=(row, row + 2),
+                          threads=O.default_threads())
             elapsed += time.perf_counter() - t0
-            row, rows = row + 1, rows + 1
+            row, rows = row + 2, rows + 2
+        thr = O.last_threads()
         cpu = {"value": round(rows * st.width * spp / elapsed / 1e6, 5), "unit": "Msamples/s", "cores": thr,
                "kind": "port", "sample": f"{rows} central rows of {st.height} at {spp} spp in {elapsed:.1f} s"}
     line = {"metric": "Msamples/s", "value": round(paths * args.steps / sec / 1e6, 2), "unit": "Msamples/s",

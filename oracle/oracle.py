@@ -67,6 +67,8 @@ def lib():
         L.orc_primary_rays.argtypes = [_u64, _u64, _u64, _f32p, _f32p, _f32p]
         L.orc_camera.argtypes = [_u64, _u64, _u64, _f32p, _f32p, _f32p]
         L.orc_trace.argtypes = [_vp, _f32p, _u64, ctypes.c_float, _i64p, _f32p, ctypes.c_int]
+        L.orc_last_threads.restype = ctypes.c_int
+        L.orc_last_threads.argtypes = []
         L.orc_render_rt.restype = _u64
         L.orc_render_rt.argtypes = [_vp, _u64, _u64, _u64, _f32p, _f32p, _f32p, ctypes.c_int, _f32p,
                                     ctypes.c_float, _u64, _u64, _u8p, ctypes.c_int]
@@ -86,6 +88,12 @@ def lib():
 
 def _f3(v) -> np.ndarray:
     return np.ascontiguousarray(np.asarray(v, np.float32).reshape(-1))
+
+
+def last_threads() -> int:
+    """Threads that OpenMP ran the most recent frame loop (render_rt /
+    render_pt) with."""
+    return int(lib().orc_last_threads())
 
 
 def default_threads() -> int:
@@ -257,6 +265,8 @@ def ref_lib(variant: str):
         L.ref_primary_rays.argtypes = [_u64, _u64, _u64, _f32p, _f32p, _f32p]
         L.ref_trace.argtypes = [_vp, _f32p, ctypes.c_size_t, _i64p, _f32p]
         L.ref_render_rt.argtypes = [_vp, _u64, _u64, _u64, _f32p, _f32p, _f32p, ctypes.c_int, _f32p, _u8p]
+        L.ref_path_moments.argtypes = [_vp, _u64, _u64, _u64, _f32p, _f32p, _f32p, _u64, _u64, ctypes.c_int, _u64,
+                                       _f64p, _f64p]
         _ref_libs[variant] = L
     return _ref_libs[variant]
 
@@ -307,6 +317,18 @@ class ReferenceScene(_TreeDumpMixin):
                              _f3(setup.cam_look), np.ascontiguousarray(lights.reshape(-1)), lights.shape[0],
                              _f3(setup.background), out)
         return out
+
+    def path_moments(self, setup, max_depth: int, runs: int, diffuse: bool = False, branching: int = 1):
+        """Per-pixel (sum, sum of squares) float64 (height, width, 3) of `runs`
+        calls of the reference's own unclamped path estimator per pixel
+        (evaluatePathRecursive, or evaluatePathRecursiveDiffuse with
+        `branching` rays per hit)."""
+        s = np.empty((setup.height, setup.width, 3), np.float64)
+        q = np.empty_like(s)
+        self.L.ref_path_moments(self._h, setup.width, setup.height, setup.fov, _f3(setup.cam_pos),
+                                _f3(setup.cam_look), _f3(setup.background), max_depth, branching,
+                                1 if diffuse else 0, runs, s, q)
+        return s, q
 
 
 def ref_primary_rays(width, height, fov, cam_pos, cam_look, variant: str = "default") -> np.ndarray:

@@ -19,6 +19,8 @@
 #include <memory>
 #include <vector>
 
+#include <omp.h>
+
 #include "../include/nostrum_pray_sampling.h"
 
 
@@ -670,9 +672,18 @@ V3 path_nee(const Scene &s, const Emitters &em, Ray r, V3 bg, uint32_t max_depth
     return L;
 }
 
+// Threads of the most recent parallel frame loop, as OpenMP ran it (not as
+// requested): the CPU baselines report this count.
+int g_last_threads = 0;
+inline void note_threads() {
+    if (omp_get_thread_num() == 0) g_last_threads = omp_get_num_threads();
+}
+
 }  // namespace
 
 extern "C" {
+
+int orc_last_threads() { return g_last_threads; }
 
 // cos/sin(2 pi u) of the shared sampling header, for accuracy tests.
 void orc_sincos_turns(const float *u, uint64_t n, float *s_out, float *c_out) {
@@ -696,9 +707,14 @@ uint64_t orc_render_pt(void *h, uint64_t w, uint64_t hh, uint64_t fov, const flo
     const Emitters em = collect_emitters(s);
     const V3 b{bg[0], bg[1], bg[2]};
     uint64_t segs = 0;
-#pragma omp parallel for schedule(dynamic, 1) reduction(+ : segs) num_threads(threads > 0 ? threads : 1)
-    for (uint64_t py = row0; py < row1; py++) {
-        for (uint64_t px = 0; px < w; px++) {
+    const int64_t npx = (int64_t)((row1 - row0) * w);
+    // pixels, not rows, are the unit of work, so that a band of a few rows
+    // still keeps every thread busy
+#pragma omp parallel for schedule(dynamic, 2) reduction(+ : segs) num_threads(threads > 0 ? threads : 1)
+    for (int64_t k = 0; k < npx; k++) {
+        note_threads();
+        {
+            const uint64_t py = row0 + (uint64_t)k / w, px = (uint64_t)k % w;
             const uint64_t pixel = py * w + px;
             const Ray prim = primary(c, px, py);
             V3 sum{0.f, 0.f, 0.f};
@@ -884,9 +900,12 @@ uint64_t orc_render_rt(void *h, uint64_t w, uint64_t hh, uint64_t fov, const flo
     V3 b{bg[0], bg[1], bg[2]};
     uint64_t shadows = 0;
     const bool empty = s.tris.empty();
-#pragma omp parallel for schedule(dynamic, 4) reduction(+ : shadows) num_threads(threads > 0 ? threads : 1)
-    for (uint64_t py = row0; py < row1; py++) {
-        for (uint64_t px = 0; px < w; px++) {
+    const int64_t npx = (int64_t)((row1 - row0) * w);
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : shadows) num_threads(threads > 0 ? threads : 1)
+    for (int64_t k = 0; k < npx; k++) {
+        note_threads();
+        {
+            const uint64_t py = row0 + (uint64_t)k / w, px = (uint64_t)k % w;
             V3 col = empty ? b : shade_rt(s, primary(c, px, py), ls, b, eps, shadows);
             uint8_t *o = out + 3 * ((py - row0) * w + px);
             o[0] = quantise(col.x);

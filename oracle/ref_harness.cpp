@@ -13,6 +13,8 @@
 //   KDTree::intersectRecursive   src/kd_tree.cpp:237-279 (private; reached with
 //                                an access override below)
 //   render / rayTrace            src/pray.cpp:380-637
+//   evaluatePathRecursive        src/pray.cpp:342-364 (Kajiya path tracer)
+//   evaluatePathRecursiveDiffuse src/pray.cpp:315-340 (branching path tracer)
 //   readSceneDescription         src/io.cpp:27-137
 #include <algorithm>
 #include <array>
@@ -40,6 +42,12 @@
 #undef protected
 
 using namespace pray;
+
+// Defined in src/pray.cpp with external linkage but not declared in its headers.
+namespace pray {
+Vec3 evaluatePathRecursive(const Ray &ray, const Scene &scene, size_t depth);
+Vec3 evaluatePathRecursiveDiffuse(const Ray &ray, const Scene &scene, size_t depth);
+}  // namespace pray
 
 namespace {
 
@@ -281,6 +289,52 @@ void ref_render_rt(void *vh, uint64_t width, uint64_t height, uint64_t fov, cons
     Image image(3 * width * height);
     render(image, s);
     std::memcpy(out, image.data(), image.size());
+}
+
+// Per-pixel moments of the reference's own path-tracing estimators on the
+// prepared scene: for every pixel, `runs` independent calls of
+// evaluatePathRecursive (diffuse == 0; src/pray.cpp:342-364, one Kajiya path
+// with max_depth bounces) or evaluatePathRecursiveDiffuse (diffuse != 0;
+// src/pray.cpp:315-340, a branching tree with `branching` rays per hit) on the
+// pixel's primary ray, unclamped. sum and sumsq (width*height*3 doubles each)
+// receive the sums of the values and of their squares. The reference seeds a
+// fresh mt19937_64 from the system clock inside every call
+// (src/pray.cpp:331,357), so these are samples of its estimator, not a
+// reproducible stream.
+void ref_path_moments(void *vh, uint64_t width, uint64_t height, uint64_t fov, const float *cam_pos,
+                      const float *cam_look, const float *bg, uint64_t max_depth, uint64_t branching,
+                      int diffuse, uint64_t runs, double *sum, double *sumsq) {
+    auto *h = static_cast<Handle *>(vh);
+    Scene &s = h->scene;
+    s.mode = Mode::PATHTRACING;
+    s.ptMode = diffuse ? PtMode::DIFFUSE : PtMode::NORMAL;
+    s.maxDepth = max_depth;
+    s.numSamples = branching;
+    s.width = width;
+    s.height = height;
+    s.field_of_view = fov;
+    s.camera_position = Vec3(cam_pos[0], cam_pos[1], cam_pos[2]);
+    s.camera_look = Vec3(cam_look[0], cam_look[1], cam_look[2]);
+    s.backgroundColor = Vec3(bg[0], bg[1], bg[2]);
+    calculatePrimRays(s);
+    const int64_t n = (int64_t)(width * height);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t i = 0; i < n; i++) {
+        double a[3] = {0, 0, 0}, q[3] = {0, 0, 0};
+        for (uint64_t k = 0; k < runs; k++) {
+            const Vec3 v = diffuse ? evaluatePathRecursiveDiffuse(s.primRays[i], s, 0)
+                                   : evaluatePathRecursive(s.primRays[i], s, 0);
+            const double c[3] = {v.x, v.y, v.z};
+            for (int j = 0; j < 3; j++) {
+                a[j] += c[j];
+                q[j] += c[j] * c[j];
+            }
+        }
+        for (int j = 0; j < 3; j++) {
+            sum[3 * i + j] = a[j];
+            sumsq[3 * i + j] = q[j];
+        }
+    }
 }
 
 }  // extern "C"

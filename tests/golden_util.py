@@ -60,3 +60,43 @@ def read_bmp(path) -> np.ndarray:
     rows = np.frombuffer(raw[off:off + pitch * abs(h)], np.uint8).reshape(abs(h), pitch)[:, :3 * w]
     img = rows.reshape(abs(h), w, 3)[:, :, ::-1]
     return np.ascontiguousarray(img if h < 0 else img[::-1])
+
+
+# -- statistical comparison of path-tracing estimators -----------------------
+
+def pt_moments_fixture():
+    """tests/golden/pt_moments.npz (make_pt_moments.py): per case, the
+    reference estimator's per-pixel mean, sample variance and run count."""
+    return dict(np.load(os.path.join(ROOT, "tests", "golden", "pt_moments.npz")))
+
+
+def batch_moments(frames):
+    """Mean and variance of the mean over independent frames (each the
+    per-pixel mean of an equal number of samples), in float64."""
+    a = np.asarray(frames, np.float64)
+    return a.mean(0), a.var(0, ddof=1) / a.shape[0]
+
+
+def same_expectation(mean_a, varmean_a, mean_b, varmean_b, max_z=6.0, z2_band=(0.6, 1.3), max_image_z=4.5):
+    """Whether two per-pixel estimates of the same image agree within their
+    sampling error. z = (a - b) / sqrt(var_a + var_b) per pixel and channel;
+    the estimates agree when no |z| exceeds max_z, the mean of z^2 lies in
+    z2_band (it is 1 for equal expectations and correctly estimated
+    variances), the image means per channel differ by less than max_image_z
+    standard errors, and pixels whose both variances are zero have equal
+    means. Returns (ok, description)."""
+    a, b = np.asarray(mean_a, np.float64), np.asarray(mean_b, np.float64)
+    va, vb = np.asarray(varmean_a, np.float64), np.asarray(varmean_b, np.float64)
+    se = np.sqrt(va + vb)
+    live = se > 0
+    dead_bad = int((np.abs(a - b)[~live] > 1e-6 * np.maximum(1.0, np.abs(a[~live]))).sum())
+    z = (a - b)[live] / se[live]
+    n_pix = a.shape[0] * a.shape[1]
+    img_z = (a.mean((0, 1)) - b.mean((0, 1))) / (np.sqrt((va + vb).sum((0, 1))) / n_pix)
+    z2 = float((z * z).mean()) if z.size else 1.0
+    zmax = float(np.abs(z).max()) if z.size else 0.0
+    ok = (dead_bad == 0 and zmax < max_z and z2_band[0] <= z2 <= z2_band[1]
+          and bool((np.abs(img_z) < max_image_z).all()))
+    desc = (f"max|z| {zmax:.2f} over {z.size}, mean z^2 {z2:.3f}, image z {np.round(img_z, 2).tolist()}, "
+            f"{dead_bad} zero-variance pixels differ")
+    return ok, desc
