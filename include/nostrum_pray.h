@@ -166,6 +166,20 @@ pray_status pray_scene_stats(const pray_scene *s, uint64_t *out);
 pray_status pray_trace_closest(pray_scene *s, const float *rays_dev, uint64_t n, float det_epsilon,
                                int32_t *ids_dev, float *t_dev, void *stream);
 
+/* pray_trace_closest for rays in host memory, for host code that asks the
+ * spatial database one ray or one batch at a time
+ * (SpatialDatabase::intersect(const Ray&, Triangle&, float&),
+ * include/spatial.h:16, which the reference's renderers call from many
+ * OpenMP threads at once). rays_host: n x 9 floats as above; ids_host and
+ * t_host receive n results. Returns when the results are in host memory.
+ * Safe to call from several host threads on the same scene: calls on one
+ * scene are serialised inside the library (one staging buffer per scene,
+ * grown on demand, freed with the scene). Every call costs a launch and two
+ * copies, so batches of thousands of rays amortise it; single rays work but
+ * are slow. */
+pray_status pray_trace_closest_host(pray_scene *s, const float *rays_host, uint64_t n, float det_epsilon,
+                                    int32_t *ids_host, float *t_host);
+
 /* Traversal of a scene's ray-traced frames: each lane walks its own ray
  * (LANES), or the warp walks its pixel tile's rays as one packet with a
  * mask of the lanes whose own box tests passed, for the primary and the
@@ -231,13 +245,15 @@ pray_status pray_accumulate_pt(pray_scene *s, const pray_pt_params *p, double *s
  * applications that must not have this library allocate device memory during
  * a frame: engines that reserve all GPU memory up front for their own pool
  * allocator, and frame loops that cannot afford cudaMalloc/cudaFree's
- * implicit device synchronisation. Same frame as pray_render_pt with
- * PRAY_SCHED_WAVEFRONT (PRAY_PT_NEE only; p->scheduler is ignored), but the
+ * implicit device synchronisation. The same frame, bit for bit, as
+ * pray_render_pt with PRAY_SCHED_WAVEFRONT (PRAY_PT_NEE only; p->scheduler is
+ * ignored; the pool may be smaller, which changes how samples are split into
+ * rounds but not the per-pixel sums, added in sample order), but the
  * path pool lives in a fixed 160 MiB static device array that every GPU
  * loading this library holds until exit; frames above 1,103,744 pixels are
  * rejected with PRAY_ERR_INVALID_ARGUMENT. Calls no cudaMalloc/cudaFree. The
- * first call on each device looks up the array's address (and may load the
- * module): make it before any stream capture. All calls share the array, so
+ * first call on each device looks up the array's address and loads every
+ * kernel a frame may launch: make it before any stream capture. All calls share the array, so
  * calls that overlap on the GPU race; order them (one stream, or events).
  * rgb_dev / radiance_dev / counters_dev as for pray_render_pt (at least one
  * of rgb_dev, radiance_dev). */

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <exception>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -120,6 +121,11 @@ struct pray_scene {
     uint64_t rgb_cap = 0;
     unsigned long long *d_counters = nullptr;
     unsigned long long *d_pt_next = nullptr;  // work counter of the per-pixel path tracer
+    // staging of pray_trace_closest_host (rays, ids, distances), grown on
+    // demand; the mutex serialises host threads that share the scene
+    std::mutex trace_mu;
+    void *d_trace = nullptr;
+    uint64_t trace_cap = 0;
 
     DevScene view() const {
         DevScene v;
@@ -149,7 +155,10 @@ struct pray_scene {
         cudaFree(d_emit_cdf);
         cudaFree(d_wf);
         cudaFree(d_pt_next);
+        cudaFree(d_trace);
         d_pt_next = nullptr;
+        d_trace = nullptr;
+        trace_cap = 0;
         if (wf_exec) cudaGraphExecDestroy(wf_exec);
         if (wf_stream) cudaStreamDestroy(wf_stream);
         if (wf_ev_in) cudaEventDestroy(wf_ev_in);
@@ -642,6 +651,38 @@ pray_status pray_trace_closest(pray_scene *s, const float *rays, uint64_t n, flo
     if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
     e = launch_trace_closest(s->view(), rays, n, eps, ids, ts, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_error(e, "trace_closest launch");
+    return PRAY_OK;
+}
+
+pray_status pray_trace_closest_host(pray_scene *s, const float *rays_host, uint64_t n, float eps, int32_t *ids_host,
+                                    float *t_host) {
+    if (!s || (n > 0 && (!rays_host || !ids_host || !t_host))) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n >= (1ull << 32)) return set_error(PRAY_ERR_INVALID_ARGUMENT, "too many rays for one call");
+    if (n == 0) return PRAY_OK;
+    std::lock_guard<std::mutex> lock(s->trace_mu);
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    // one buffer: n x 9 floats of rays, then n ids, then n distances (all 4-byte words)
+    if (n > s->trace_cap) {
+        cudaFree(s->d_trace);
+        s->d_trace = nullptr;
+        s->trace_cap = 0;
+        const uint64_t cap = std::max<uint64_t>(n, 1024);
+        if ((e = cudaMalloc(&s->d_trace, cap * 11 * sizeof(float))) != cudaSuccess)
+            return cuda_error(e, "cudaMalloc (trace staging)");
+        s->trace_cap = cap;
+    }
+    float *d_rays = static_cast<float *>(s->d_trace);
+    int32_t *d_ids = reinterpret_cast<int32_t *>(d_rays + 9 * s->trace_cap);
+    float *d_t = reinterpret_cast<float *>(d_ids + s->trace_cap);
+    if ((e = cudaMemcpy(d_rays, rays_host, n * 9 * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cuda_error(e, "cudaMemcpy (rays)");
+    if ((e = launch_trace_closest(s->view(), d_rays, n, eps, d_ids, d_t, 0)) != cudaSuccess)
+        return cuda_error(e, "trace_closest launch");
+    if ((e = cudaMemcpy(ids_host, d_ids, n * sizeof(int32_t), cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return cuda_error(e, "cudaMemcpy (ids)");
+    if ((e = cudaMemcpy(t_host, d_t, n * sizeof(float), cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return cuda_error(e, "cudaMemcpy (distances)");
     return PRAY_OK;
 }
 

@@ -72,6 +72,10 @@ uint64_t wavefront_scratch_bytes(uint64_t capacity, uint64_t pixels);
 // Carves a scratch block of wavefront_scratch_bytes() bytes (256-byte aligned base).
 WavefrontScratch wavefront_carve(void *base, uint64_t capacity, uint64_t pixels);
 // Enqueues one whole frame (all rounds) on `stream`; capturable in a graph.
+// Loads every kernel a wavefront frame may launch (both traversal-stack
+// variants) on the current device, so that no later frame triggers a lazy
+// module load.
+cudaError_t wavefront_preload_kernels();
 cudaError_t record_wavefront_frame(const DevScene &s, const PtLaunch &L, const WavefrontScratch &w, int sm_count,
                                    cudaStream_t stream);
 

@@ -392,6 +392,20 @@ WavefrontScratch wavefront_carve(void *base, uint64_t capacity, uint64_t pixels)
     return w;
 }
 
+cudaError_t wavefront_preload_kernels() {
+    cudaFuncAttributes a;
+    const void *kernels[] = {
+        reinterpret_cast<const void *>(k_wf_init),         reinterpret_cast<const void *>(k_wf_extend<32>),
+        reinterpret_cast<const void *>(k_wf_extend<kStack>), reinterpret_cast<const void *>(k_wf_shade),
+        reinterpret_cast<const void *>(k_wf_occlude<32>),  reinterpret_cast<const void *>(k_wf_occlude<kStack>),
+        reinterpret_cast<const void *>(k_wf_accumulate),   reinterpret_cast<const void *>(k_wf_finish)};
+    for (const void *k : kernels) {
+        cudaError_t e = cudaFuncGetAttributes(&a, k);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t record_wavefront_frame(const DevScene &s, const PtLaunch &L, const WavefrontScratch &w, int sm_count,
                                    cudaStream_t stream) {
     const uint64_t P = (uint64_t)L.cam.width * L.cam.height;

@@ -13,7 +13,9 @@
 // Host code cannot use the array's name as a device address; the first call on
 // each device looks the address up with cudaGetSymbolAddress (with that device
 // current) and caches it, and every launch gets the address as a parameter.
-// That first call may load the module; make it before any stream capture.
+// The same first call also loads every kernel a frame may launch (both
+// traversal-stack depths), so module loading happens there and nowhere later;
+// make that first call before any stream capture.
 //
 // All calls share the one array and it keeps the last call's contents. Nothing
 // in it needs to start at zero: the init pass of every round writes all path
@@ -78,6 +80,11 @@ cudaError_t launch_wavefront_noalloc(const DevScene &s, const PtLaunch &L, uint6
             int n = 0;
             e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
             if (e != cudaSuccess) return e;
+            e = wavefront_preload_kernels();
+            if (e != cudaSuccess) {
+                why = "loading the wavefront kernels failed";
+                return e;
+            }
             g_scratch_addr[dev] = p;
             g_sm_count[dev] = n;
         }

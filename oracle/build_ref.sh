@@ -12,21 +12,35 @@
 # geometry.h EPSILON) are patched into a temporary copy of its include/
 # directory under /tmp, which is removed afterwards.
 #
-# Usage: oracle/build_ref.sh [variant ...]   (default: all variants)
+# It also compiles the reference-side binding (integration/gpu_kdtree.cpp)
+# against the reference's own headers, once per instruction set the
+# reference's include/options.h distinguishes (scalar, and on x86 also SSE3
+# and AVX), into oracle/_ref/gpu_kdtree_<isa>.o, and records the reference's
+# location in oracle/_ref/ref_root.txt for the tests that read its example
+# scenes.
+#
+# The scalar build is portable C++ (include/options.h picks the plain code
+# without __AVX__ / __SSE3__), so it is built on any host; only the AVX
+# timing variant is x86-only.
+#
+# Usage: REF_ROOT=<reference checkout> oracle/build_ref.sh [variant ...]
+#        (default: all parity variants)
 set -euo pipefail
-REF="${REF_ROOT:-/root/reference}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
+if [ -z "${REF_ROOT:-}" ]; then
+    echo "build_ref: REF_ROOT is not set; nothing built"
+    exit 0
+fi
+REF="$REF_ROOT"
 
 if [ ! -d "$REF/src" ] || [ ! -d "$REF/include" ]; then
     echo "build_ref: reference sources not found at $REF; nothing built"
     exit 0
 fi
-if [ "$(uname -m)" != "x86_64" ]; then
-    echo "build_ref: parity build expects an x86_64 host; nothing built"
-    exit 0
-fi
 mkdir -p "$OUT"
+echo "$REF" > "$OUT/ref_root.txt"
+ARCH="$(uname -m)"
 
 # name leaf max_depth sah_traversal_cost det_epsilon
 VARIANTS=(
@@ -69,8 +83,32 @@ build_variant() {
     echo "build_ref: built $lib"
 }
 
+build_binding() {
+    local isa=$1 flags=$2
+    local obj="$OUT/gpu_kdtree_${isa}.o"
+    local src="$HERE/../integration/gpu_kdtree.cpp"
+    if [ -f "$obj" ] && [ "$obj" -nt "$src" ] && [ "$obj" -nt "$HERE/../integration/gpu_kdtree.h" ] &&
+       [ "$obj" -nt "$HERE/../include/nostrum_pray.h" ]; then
+        return 0
+    fi
+    g++ -std=c++14 $flags -O1 -fPIC -Wall -Wextra -Wno-reorder -include limits -include fstream \
+        -I"$REF/include" -I"$REF/ext" -I"$HERE/../include" -c "$src" -o "$obj.tmp"
+    mv "$obj.tmp" "$obj"
+    echo "build_ref: built $obj"
+}
+
 want=("$@")
 pids=()
+if [ ${#want[@]} -eq 0 ]; then
+    build_binding scalar "" &
+    pids+=($!)
+    if [ "$ARCH" = "x86_64" ]; then
+        build_binding sse "-msse3" &
+        pids+=($!)
+        build_binding avx "-mavx" &
+        pids+=($!)
+    fi
+fi
 for v in "${VARIANTS[@]}"; do
     set -- $v
     if [ ${#want[@]} -eq 0 ] || printf '%s\n' "${want[@]}" | grep -qx "$1"; then
@@ -80,7 +118,7 @@ for v in "${VARIANTS[@]}"; do
 done
 for v in "${TIMING_VARIANTS[@]}"; do
     set -- $v
-    if [ ${#want[@]} -gt 0 ] && printf '%s\n' "${want[@]}" | grep -qx "$1"; then
+    if [ "$ARCH" = "x86_64" ] && [ ${#want[@]} -gt 0 ] && printf '%s\n' "${want[@]}" | grep -qx "$1"; then
         build_variant "$1" "$2" "$3" "$4" "$5" "${*:6}" &
         pids+=($!)
     fi

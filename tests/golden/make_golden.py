@@ -12,6 +12,7 @@ reference's example scenes, and stores what it returns:
   at 1920x1080), whose arrays are too large to commit.
 
 Usage (needs the reference sources; writes only into this directory):
+    export REF_ROOT=<reference checkout>
     oracle/build_ref.sh && python tests/golden/make_golden.py
 """
 from __future__ import annotations
@@ -31,7 +32,7 @@ sys.path.insert(0, ROOT)
 from nostrum_pray_gb300 import scenes  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
-REF_ROOT = os.environ.get("REF_ROOT", "/root/reference")
+REF_ROOT = os.environ.get("REF_ROOT", "")
 
 
 def sha(a: np.ndarray) -> str:
@@ -55,6 +56,8 @@ def trace_case(ref, setup):
 
 
 def main():
+    if not os.path.isdir(os.path.join(REF_ROOT, "examples")):
+        sys.exit("make_golden: set REF_ROOT to a checkout of the reference")
     small = {}
     hashes = {}
 

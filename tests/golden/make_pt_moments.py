@@ -21,7 +21,7 @@ in golden_small.npz under ex_pt_cornell_*), at reduced resolutions with each
 scene's own camera.
 
 Usage (needs oracle/_ref built from the reference sources):
-    oracle/build_ref.sh && python tests/golden/make_pt_moments.py
+    REF_ROOT=<reference checkout> oracle/build_ref.sh && python tests/golden/make_pt_moments.py
 """
 from __future__ import annotations
 

@@ -11,6 +11,18 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 BUILD = os.path.join(ROOT, "nostrum_pray_gb300", "_build")
 
 
+def ref_root():
+    """A checkout of the reference, for tests that read its files: REF_ROOT
+    from the environment, else the location oracle/build_ref.sh recorded
+    when it built the reference; None where there is none."""
+    r = os.environ.get("REF_ROOT")
+    if not r:
+        rec = os.path.join(ROOT, "oracle", "_ref", "ref_root.txt")
+        if os.path.exists(rec):
+            r = open(rec).read().strip()
+    return r if r and os.path.isdir(os.path.join(r, "include")) else None
+
+
 def sha(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 

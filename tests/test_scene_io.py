@@ -9,13 +9,13 @@ import tempfile
 import numpy as np
 import pytest
 
-from golden_util import load_scene_dump
+from golden_util import load_scene_dump, ref_root
 from nostrum_pray_gb300 import scenes
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 DUMP = os.path.join(ROOT, "nostrum_pray_gb300", "_build", "pray_scene_dump")
 CASES = os.path.join(ROOT, "tests", "golden", "obj_cases")
-REF_EXAMPLES = os.path.join(os.environ.get("REF_ROOT", "/root/reference"), "examples")
+REF_EXAMPLES = os.path.join(ref_root() or "", "examples")
 
 
 @pytest.fixture(scope="module", autouse=True)

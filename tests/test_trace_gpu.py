@@ -276,3 +276,34 @@ def test_distant_origins(oracle, dist):
     assert (wid >= 0).sum() > n // 3
     assert int((ids != wid.astype(np.int32)).sum()) == 0
     np.testing.assert_array_equal(ts.view(np.uint32), wt.view(np.uint32))
+
+
+def test_host_rays_from_many_threads(oracle):
+    """pray_trace_closest_host, the entry point behind the reference-side
+    SpatialDatabase::intersect binding: host rays in, host ids and distances
+    out, called concurrently from eight host threads on one scene (the
+    reference's renderers query the database from OpenMP threads), with
+    batches of one ray up to whole frames; bit-exact against the oracle."""
+    from concurrent.futures import ThreadPoolExecutor
+    mesh = scenes.soup(10_000, 2)
+    st = scenes.soup_setup(96, 80)
+    sc = native.Scene.from_setup(mesh, st)
+    rays = oracle.primary_rays(st.width, st.height, st.fov, st.cam_pos, st.cam_look)
+    want_ids, want_t = oracle.OracleScene.from_setup(mesh, st).trace(rays, st.det_eps)
+    sizes = [1, 7, 64, 1000, rays.shape[0]]
+
+    def job(k):
+        n = sizes[k % len(sizes)]
+        lo = (k * 977) % (rays.shape[0] - n + 1)
+        ids, ts = sc.trace_closest_host(rays[lo:lo + n], st.det_eps)
+        return lo, n, ids, ts
+
+    with ThreadPoolExecutor(8) as ex:
+        results = list(ex.map(job, range(64)))
+    for lo, n, ids, ts in results:
+        np.testing.assert_array_equal(ids, want_ids[lo:lo + n].astype(np.int32))
+        np.testing.assert_array_equal(ts.view(np.uint32), want_t[lo:lo + n].view(np.uint32))
+    assert int((want_ids >= 0).sum()) > 1000
+    ids, ts = sc.trace_closest_host(rays[:0], st.det_eps)
+    assert ids.size == 0
+    sc.close()
