@@ -54,6 +54,19 @@ __device__ __forceinline__ RayF make_ray(float ox, float oy, float oz, float dx,
     return r;
 }
 
+// Three-input minimum / maximum (one instruction on sm_100 and later). Like
+// fminf / fmaxf, a NaN operand is ignored unless all are NaN.
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 // BoundingBox::intersect, include/geometry.h:151-164. `finite`: all three
 // inverse direction components are finite, so no slab value can be NaN; then
 // fminf/fmaxf return the same values as the reference's std::min/std::max
@@ -66,8 +79,9 @@ __device__ __forceinline__ bool slab(const float4 &lo, const float4 &hi, const R
     const float t1y = (lo.y - r.oy) * r.iy, t2y = (hi.y - r.oy) * r.iy;
     const float t1z = (lo.z - r.oz) * r.iz, t2z = (hi.z - r.oz) * r.iz;
     if (finite) {
-        tn = fmaxf(fmaxf(fminf(t1x, t2x), fminf(t1y, t2y)), fmaxf(fminf(t1z, t2z), -FLT_MAX));
-        tf = fminf(fminf(fmaxf(t1x, t2x), fmaxf(t1y, t2y)), fminf(fmaxf(t1z, t2z), FLT_MAX));
+        // the same values as fmaxf(fmaxf(a, b), fmaxf(c, -FLT_MAX)) and its mirror
+        tn = max3f(fminf(t1x, t2x), fminf(t1y, t2y), fmaxf(fminf(t1z, t2z), -FLT_MAX));
+        tf = min3f(fmaxf(t1x, t2x), fmaxf(t1y, t2y), fminf(fmaxf(t1z, t2z), FLT_MAX));
     } else {
         tn = smax(smax(smin(t1x, t2x), smin(t1y, t2y)), smax(smin(t1z, t2z), -FLT_MAX));
         tf = smin(smin(smax(t1x, t2x), smax(t1y, t2y)), smin(smax(t1z, t2z), FLT_MAX));
@@ -89,13 +103,20 @@ __device__ __forceinline__ bool slab(const float4 &lo, const float4 &hi, const R
 // entry and exit alike: the pad still holds the triangle hits it was sized
 // for (host/flatten.cpp), so no box that the exact ray crosses around a hit
 // fails the test or the pruning bound.
+//
+// Entry and exit take the three-input min / max and drop the reference's clamps to
+// -FLT_MAX / FLT_MAX: with a finite inverse direction and finite o * inv no
+// plane distance of a finite box is NaN, so the clamps change only an
+// infinite entry or exit into FLT_MAX, which no comparison here sees. Boxes of
+// empty leaves (infinite or NaN coordinates, no triangles) may then fail where
+// they passed before, which drops no triangle.
 __device__ __forceinline__ bool slab_fma(const float4 &lo, const float4 &hi, const RayF &r, float nox, float noy,
                                          float noz, float &tn, float &tf) {
     const float t1x = fmaf(lo.x, r.ix, nox), t2x = fmaf(hi.x, r.ix, nox);
     const float t1y = fmaf(lo.y, r.iy, noy), t2y = fmaf(hi.y, r.iy, noy);
     const float t1z = fmaf(lo.z, r.iz, noz), t2z = fmaf(hi.z, r.iz, noz);
-    tn = fmaxf(fmaxf(fminf(t1x, t2x), fminf(t1y, t2y)), fmaxf(fminf(t1z, t2z), -FLT_MAX));
-    tf = fminf(fminf(fmaxf(t1x, t2x), fmaxf(t1y, t2y)), fminf(fmaxf(t1z, t2z), FLT_MAX));
+    tn = max3f(fminf(t1x, t2x), fminf(t1y, t2y), fminf(t1z, t2z));
+    tf = min3f(fmaxf(t1x, t2x), fmaxf(t1y, t2y), fmaxf(t1z, t2z));
     return tn <= tf;
 }
 

@@ -12,7 +12,9 @@
 # geometry.h EPSILON) are patched into a temporary copy of its include/
 # directory under /tmp, which is removed afterwards.
 #
-# It also compiles the reference-side binding (integration/gpu_kdtree.cpp)
+# It also compiles the reference's GPU path tracer (src/path_trace.cu, device
+# code only) into oracle/_ref/prayref_path_trace.cubin for sm_103a, and the
+# reference-side binding (integration/gpu_kdtree.cpp)
 # against the reference's own headers, once per instruction set the
 # reference's include/options.h distinguishes (scalar, and on x86 also SSE3
 # and AVX), into oracle/_ref/gpu_kdtree_<isa>.o, and records the reference's
@@ -76,7 +78,7 @@ build_variant() {
         -include limits -include fstream \
         -I"$tmp/include" -I"$REF/ext" \
         "$REF/src/kd_tree.cpp" "$REF/src/kd_tree_sah.cpp" "$REF/src/geometry.cpp" "$REF/src/geometry_simd.cpp" \
-        "$REF/src/scene_preprocessor.cpp" "$REF/src/pray.cpp" "$REF/src/io.cpp" \
+        "$REF/src/scene_preprocessor.cpp" "$REF/src/pray.cpp" "$REF/src/io.cpp" "$REF/src/gpu_util.cpp" \
         "$HERE/ref_harness.cpp" -o "$lib.tmp" -lstdc++fs
     mv "$lib.tmp" "$lib"
     rm -rf "$tmp"
@@ -97,9 +99,26 @@ build_binding() {
     echo "build_ref: built $obj"
 }
 
+# The reference's GPU path tracer (src/path_trace.cu) as an sm_103a cubin,
+# device code only, for oracle/ref_gpu_launch.cpp to load and time.
+build_cubin() {
+    local cubin="$OUT/prayref_path_trace.cubin"
+    command -v nvcc >/dev/null 2>&1 || return 0
+    if [ -f "$cubin" ] && [ "$cubin" -nt "$0" ]; then
+        return 0
+    fi
+    nvcc -cubin -gencode arch=compute_103a,code=sm_103a -O3 -std=c++14 -include limits -include fstream \
+        -diag-suppress 20012,20013,20015 -I"$REF/include" -I"$REF/ext" -DWITH_CUDA \
+        "$REF/src/path_trace.cu" -o "$cubin.tmp"
+    mv "$cubin.tmp" "$cubin"
+    echo "build_ref: built $cubin"
+}
+
 want=("$@")
 pids=()
 if [ ${#want[@]} -eq 0 ]; then
+    build_cubin &
+    pids+=($!)
     build_binding scalar "" &
     pids+=($!)
     if [ "$ARCH" = "x86_64" ]; then

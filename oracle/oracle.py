@@ -265,6 +265,8 @@ def ref_lib(variant: str):
         L.ref_primary_rays.argtypes = [_u64, _u64, _u64, _f32p, _f32p, _f32p]
         L.ref_trace.argtypes = [_vp, _f32p, ctypes.c_size_t, _i64p, _f32p]
         L.ref_render_rt.argtypes = [_vp, _u64, _u64, _u64, _f32p, _f32p, _f32p, ctypes.c_int, _f32p, _u8p]
+        L.ref_gpu_tree_size.argtypes = [_vp, _u64p, _u64p]
+        L.ref_gpu_tree.argtypes = [_vp, _i32p, _i32p, _u8p, _u64p, _u64p, _f32p, _u8p, _f32p, _i32p, _u64p]
         L.ref_path_moments.argtypes = [_vp, _u64, _u64, _u64, _f32p, _f32p, _f32p, _u64, _u64, ctypes.c_int, _u64,
                                        _f64p, _f64p]
         _ref_libs[variant] = L
@@ -317,6 +319,22 @@ class ReferenceScene(_TreeDumpMixin):
                              _f3(setup.cam_look), np.ascontiguousarray(lights.reshape(-1)), lights.shape[0],
                              _f3(setup.background), out)
         return out
+
+    def gpu_tree(self):
+        """The reference's breadth-first GPU tree (buildGPUTreeFromKDTree) as
+        a dict of per-node fields and the leaf index array. Consumes the
+        scene: the reference moves the triangles out of its tree."""
+        nn, ni = np.zeros(1, np.uint64), np.zeros(1, np.uint64)
+        self.L.ref_gpu_tree_size(self._h, nn, ni)
+        n, m = int(nn[0]), int(ni[0])
+        out = {"left": np.empty(n, np.int32), "right": np.empty(n, np.int32), "is_leaf": np.empty(n, np.uint8),
+               "first": np.empty(n, np.uint64), "count": np.empty(n, np.uint64),
+               "box": np.empty((n, 6), np.float32), "axis": np.empty(n, np.uint8), "split": np.empty(n, np.float32),
+               "ropes": np.empty((n, 6), np.int32)}
+        idx = np.empty(max(m, 1), np.uint64)
+        self.L.ref_gpu_tree(self._h, out["left"], out["right"], out["is_leaf"], out["first"], out["count"], out["box"],
+                            out["axis"], out["split"], out["ropes"], idx)
+        return out, idx[:m]
 
     def path_moments(self, setup, max_depth: int, runs: int, diffuse: bool = False, branching: int = 1):
         """Per-pixel (sum, sum of squares) float64 (height, width, 3) of `runs`

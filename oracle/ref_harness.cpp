@@ -13,6 +13,8 @@
 //   KDTree::intersectRecursive   src/kd_tree.cpp:237-279 (private; reached with
 //                                an access override below)
 //   render / rayTrace            src/pray.cpp:380-637
+//   buildGPUTreeFromKDTree       src/gpu_util.cpp:7-57 (device layout of the
+//                                reference's GPU path tracer)
 //   evaluatePathRecursive        src/pray.cpp:342-364 (Kajiya path tracer)
 //   evaluatePathRecursiveDiffuse src/pray.cpp:315-340 (branching path tracer)
 //   readSceneDescription         src/io.cpp:27-137
@@ -38,6 +40,7 @@
 #include "kd_tree_sah.h"
 #include "scene_preprocessor.h"
 #include "io.h"
+#include "gpu_util.h"
 #undef private
 #undef protected
 
@@ -335,6 +338,44 @@ void ref_path_moments(void *vh, uint64_t width, uint64_t height, uint64_t fov, c
             sumsq[3 * i + j] = q[j];
         }
     }
+}
+
+// The breadth-first device tree of the reference's GPU path tracer
+// (buildGPUTreeFromKDTree) over the prepared median tree, field by field:
+// per node left, right (int32), is_leaf (uint8), first, count (uint64),
+// box[6] (float), axis (uint8), split (float), ropes[6] (int32); indices: the
+// concatenated leaf triangle indices. Call ref_gpu_tree_size first for the
+// sizes. The reference moves the tree's triangles into its result, so the
+// handle is not usable afterwards.
+void ref_gpu_tree_size(void *vh, uint64_t *n_nodes, uint64_t *n_indices) {
+    auto *h = static_cast<Handle *>(vh);
+    const KDTree &t = tree_of(h);
+    *n_nodes = t.nnodes;
+    uint64_t refs = 0;
+    std::vector<const KDTreeElement *> order;
+    dfs_dump(t.root.get(), order);
+    for (auto *n : order) refs += n->triangleIndices.size();
+    *n_indices = refs;
+}
+
+void ref_gpu_tree(void *vh, int32_t *left, int32_t *right, uint8_t *is_leaf, uint64_t *first, uint64_t *count,
+                  float *box, uint8_t *axis, float *split, int32_t *ropes, uint64_t *indices) {
+    auto *h = static_cast<Handle *>(vh);
+    KDTreeGPU g = buildGPUTreeFromKDTree(h->scene.triangleDB);
+    for (size_t i = 0; i < g.nodes.size(); i++) {
+        const KDTreeGPUNode &n = g.nodes[i];
+        left[i] = n.leftChildIndex;
+        right[i] = n.rightChildIndex;
+        is_leaf[i] = n.isLeaf ? 1 : 0;
+        first[i] = n.firstTriangleIdxIdx;
+        count[i] = n.numTriangles;
+        const float b[6] = {n.bb.min.x, n.bb.min.y, n.bb.min.z, n.bb.max.x, n.bb.max.y, n.bb.max.z};
+        for (int k = 0; k < 6; k++) box[6 * i + k] = b[k];
+        axis[i] = n.splitPlane.axis;
+        split[i] = n.splitPlane.distance;
+        for (int k = 0; k < 6; k++) ropes[6 * i + k] = n.ropes[k];
+    }
+    for (size_t i = 0; i < g.triangleIndices.size(); i++) indices[i] = g.triangleIndices[i];
 }
 
 }  // extern "C"

@@ -1,0 +1,54 @@
+"""This library's path tracer next to the reference's own GPU path tracer
+(GPU).
+
+evaluatePathKernelDiffuse / evaluatePathKernel of src/path_trace.cu, compiled
+from the reference's sources into an sm_103a cubin (oracle/build_ref.sh), run
+through oracle/ref_gpu.py with the inputs the reference's host code would
+give them (pinned by tests/test_ref_gpu_layout_cpu.py). The reference draws
+from curand streams seeded per pixel, this library from PCG32 streams, so the
+frames are compared as estimates of the same image: on the reference's
+examples/pt_cornell scene as shipped (branching mode, max_depth 1, 4,000 rays
+per hit) at 80 x 60, the quantised frames must have the same mean per
+channel within 0.5 (of 255) and differ by more than 8 at under 0.5 % of the
+values. Skipped where the cubin was not built (no reference sources where the
+repository was prepared)."""
+import numpy as np
+import pytest
+
+from golden import make_pt_moments as M
+from nostrum_pray_gb300 import native, scenes
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    native.lib()
+
+
+def cornell(w, h):
+    mesh, st = M.case_scene("cornell_diffuse1")
+    st = scenes.RenderSetup(**{**st.__dict__, "width": w, "height": h})
+    return mesh, st
+
+
+@pytest.mark.parametrize("diffuse,depth,n,mean_tol,big", [(True, 1, 4000, 0.5, 8)])
+def test_same_image_as_reference_gpu_kernel(diffuse, depth, n, mean_tol, big):
+    from oracle import ref_gpu as G
+    if not G.available():
+        pytest.skip("the reference's GPU path tracer was not built (no reference sources)")
+    mesh, st = cornell(80, 60)
+    ref_img, ms = G.render(mesh, st, depth, n, diffuse)
+    assert ms > 0
+    st_ours = scenes.RenderSetup(**{**st.__dict__, "tree": "median", "det_eps": 1e-4})
+    sc = native.Scene.from_setup(mesh, st_ours)
+    mode = native.PT_DIFFUSE if diffuse else native.PT_KAJIYA
+    img, _, _ = sc.render_pt_host(native.pt_params(st_ours, spp=n, max_depth=depth, seed=5, mode=mode))
+    d = img.astype(np.float64) - ref_img.astype(np.float64)
+    assert ref_img.mean() > 20, "the reference's frame is dark: wrong inputs?"
+    assert np.abs(d.mean((0, 1))).max() < mean_tol, d.mean((0, 1))
+    assert (np.abs(d) > big).mean() < 0.005, (np.abs(d) > big).mean()
+    sc.close()
