@@ -19,8 +19,6 @@
 
 #include <cstdint>
 
-#include <vector_types.h>
-
 namespace pray_gpu {
 
 constexpr uint32_t kLeafFlag = 0x80000000u;
@@ -47,18 +45,6 @@ struct alignas(16) GShade {
     float c[4];
 };
 
-// Split records of the culling copy (8 bytes per node, same slots as the
-// GNode copy), for the warp-packet walk over SAH voxel trees. Where a node's
-// children are exactly its voxel cut by one axis-aligned plane, a visit needs
-// only that plane: each lane clips its own entry/exit interval at the plane's
-// distance instead of testing two boxes.
-//   split node:   x = split position (float bits), y = axis << 30 | index of the children's pair
-//   linear leaf:  x = first triangle reference,    y = 3 << 30 | reference count
-//   box node:     x = index of the children's pair (their boxes in the GNode copy), y = 3 << 30 | 1 << 29
-constexpr uint32_t kKindBox = 3u << 30;
-constexpr uint32_t kKindBoxInterior = 1u << 29;
-constexpr uint32_t kKdCountMask = kKindBoxInterior - 1u;
-
 // Launch-time view of a device scene.
 struct DevScene {
     const GNode *nodes;  // n_nodes nodes with the reference's boxes and linear leaves, then the culling
@@ -76,11 +62,6 @@ struct DevScene {
     const float *emit_cdf;
     uint32_t n_emit;
     float emit_area;
-    // split records of the culling copy (n_nodes of them), or NULL where the
-    // tree has no split nodes (median trees); kd_pad = 2^-16 of the scene's
-    // diagonal, the absolute part of a split plane's padding
-    const uint2 *knodes;
-    float kd_pad;
 };
 
 }  // namespace pray_gpu

@@ -45,7 +45,6 @@ struct Flattener {
     float pad_scene = 0.f;                            // kPadScene x the scene's diagonal
     std::vector<std::pair<uint32_t, Tight>> tight{};  // interior reference nodes: slot, padded triangle bounds
     std::vector<std::pair<uint32_t, GNode>> linear{};  // refined reference leaves: slot, linear leaf over the same range
-    std::vector<std::pair<uint32_t, uint2>> splits{};  // reference interior nodes in split form: slot, record
 
     uint32_t alloc_pair() {
         const uint32_t pair = (uint32_t)out.nodes.size();
@@ -132,24 +131,6 @@ struct Flattener {
         out.nodes[slot].a = pair;
     }
 
-    // Whether the children of interior node p are its box cut at its split
-    // plane, exactly.
-    bool is_voxel_split(int32_t p) const {
-        const FlatNode &n = t.nodes[p];
-        if (n.left < 0 || n.right < 0 || n.axis < 0 || n.axis > 2 || !std::isfinite(n.split)) return false;
-        const Aabb &b = n.box, &l = t.nodes[n.left].box, &r = t.nodes[n.right].box;
-        for (int k = 0; k < 3; k++) {
-            const float llo = b.lo[k], lhi = k == n.axis ? n.split : b.hi[k];
-            const float rlo = k == n.axis ? n.split : b.lo[k], rhi = b.hi[k];
-            if (std::memcmp(&l.lo[k], &llo, 4) || std::memcmp(&l.hi[k], &lhi, 4) || std::memcmp(&r.lo[k], &rlo, 4) ||
-                std::memcmp(&r.hi[k], &rhi, 4))
-                return false;
-            if (!std::isfinite(b.lo[k]) || !std::isfinite(b.hi[k])) return false;
-        }
-        return pair_ok(n);
-    }
-    static bool pair_ok(const FlatNode &) { return true; }
-
     // Reference node p into slot (the box is the reference's, unpadded).
     // Returns the padded bounds of the triangles below it; for an interior
     // node they are recorded in tight[slot].
@@ -184,11 +165,6 @@ struct Flattener {
         out.nodes[slot] = g;
         const uint32_t pair = alloc_pair();
         out.nodes[slot].a = pair;
-        if (is_voxel_split(p)) {
-            uint32_t bits;
-            std::memcpy(&bits, &n.split, 4);
-            splits.push_back({slot, make_uint2(bits, ((uint32_t)n.axis << 30) | pair)});
-        }
         const Tight l = put(n.left, pair, depth + 1);
         const Tight r = put(n.right, pair + 1, depth + 1);
         Tight b;
@@ -238,19 +214,6 @@ void flatten_for_device(const BuiltTree &t, const std::vector<TriPre> &pre, int 
         if (!usable || !(area(b.lo, b.hi) < area(g.lo, g.hi))) continue;
         for (int k = 0; k < 3; k++) g.lo[k] = b.lo[k], g.hi[k] = b.hi[k];
     }
-    // split records of the culling copy: split form where the reference's
-    // voxels allow it, the GNode payload elsewhere
-    out.knodes.clear();
-    out.split_nodes = f.splits.size();
-    out.kd_pad = f.pad_scene;
-    if (f.splits.empty()) return;
-    out.knodes.resize(out.nodes_tight.size());
-    for (size_t i = 0; i < out.nodes_tight.size(); i++) {
-        const GNode &g = out.nodes_tight[i];
-        if (g.b & kLeafFlag) out.knodes[i] = make_uint2(g.a, kKindBox | (g.b & ~kLeafFlag));
-        else out.knodes[i] = make_uint2(g.a, kKindBox | kKindBoxInterior);
-    }
-    for (const auto &[slot, k] : f.splits) out.knodes[slot] = k;
 }
 
 namespace {

@@ -31,14 +31,6 @@
 //   the padded triangle bounds do. Leaves keep the reference's box.
 // Rays with an infinite inverse component (NaN cases of the reference's test)
 // or a distant origin use the exact copy.
-//
-// Split records (knodes): a reference interior node whose children's boxes
-// are its own box with hi[axis] (left) and lo[axis] (right) replaced by the
-// split position, bit for bit (every SAH voxel split), gets an 8-byte split
-// record; every other slot records its GNode payload. A packet walk over the
-// split records clips each ray's interval at the plane, padded on both sides
-// by 2^-15 |split| + 2^-16 D: the same pad as the culling boxes' planes, so a
-// leaf voxel reached this way is its box padded as a culling box would be.
 #pragma once
 
 #include <cstdint>
@@ -57,11 +49,6 @@ struct DeviceImage {
     float cull_center[3] = {0.f, 0.f, 0.f};
     float cull_radius2 = -1.f;  // origins within sqrt of this of cull_center may use nodes_tight
     std::vector<GTri> tris;
-    // split records of the culling copy (device_layout.h), one per slot; empty
-    // when no node of the tree is a split node
-    std::vector<uint2> knodes;
-    uint64_t split_nodes = 0;     // culling-copy nodes in split form
-    float kd_pad = 0.f;           // 2^-16 of the scene's diagonal
     uint64_t refined_leaves = 0;  // reference leaves split into a sub-hierarchy
     uint64_t sub_nodes = 0;       // nodes added by the refinement
 };

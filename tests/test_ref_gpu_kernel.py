@@ -8,10 +8,19 @@ give them (pinned by tests/test_ref_gpu_layout_cpu.py). The reference draws
 from curand streams seeded per pixel, this library from PCG32 streams, so the
 frames are compared as estimates of the same image: on the reference's
 examples/pt_cornell scene as shipped (branching mode, max_depth 1, 4,000 rays
-per hit) at 80 x 60, the quantised frames must have the same mean per
-channel within 0.5 (of 255) and differ by more than 8 at under 0.5 % of the
-values. Skipped where the cubin was not built (no reference sources where the
-repository was prepared)."""
+per hit) at 80 x 60, and in Kajiya mode at max_depth 1 (1,024 paths per
+pixel), the quantised frames must have the same mean per channel within 0.5
+(of 255) and differ by more than 8 at under 0.5 % of the values.
+
+At max_depth 2 and beyond the reference's GPU Kajiya kernel loses energy: at
+80 x 60 with 1,024 paths per pixel its image mean is 64.4 (of 255, red) at
+depth 1, 67.7 at depth 2 and 37.4 / 35.8 at depths 3 / 4, darker than at
+depth 1, which no unbiased estimator of a scene without negative light can
+be; the reference's own CPU estimator (evaluatePathRecursive, against which
+this library's Kajiya mode is pinned statistically in test_pt_stats_gpu.py)
+grows with depth as expected (ours 64.3, 73.2, 77.1, 79.0). So Kajiya frames
+are compared at depth 1 only. Skipped where the cubin was not built (no
+reference sources where the repository was prepared)."""
 import numpy as np
 import pytest
 
@@ -35,7 +44,7 @@ def cornell(w, h):
     return mesh, st
 
 
-@pytest.mark.parametrize("diffuse,depth,n,mean_tol,big", [(True, 1, 4000, 0.5, 8)])
+@pytest.mark.parametrize("diffuse,depth,n,mean_tol,big", [(True, 1, 4000, 0.5, 8), (False, 1, 1024, 0.5, 8)])
 def test_same_image_as_reference_gpu_kernel(diffuse, depth, n, mean_tol, big):
     from oracle import ref_gpu as G
     if not G.available():
