@@ -556,10 +556,10 @@ def run_denoise(args):
     t0 = time.perf_counter()
     train_seeds = list(range(cfg.seed, cfg.seed + cfg.train_rooms))
     eval_seeds = list(range(cfg.seed + 100_000, cfg.seed + 100_000 + cfg.eval_rooms))
-    _, rad, feat, ref = D.make_dataset(cfg, train_seeds, torch, cfg.train_res)
-    # held-out rooms are judged against references with more samples (the error target's yardstick)
+    _, rad, feat, ref = D.make_dataset(cfg, train_seeds, torch, cfg.train_res, keep_scenes=False)
+    # held-out rooms are judged against references with more samples (the error target's yardstick),
+    # rendered one at a time during the evaluation
     eval_cfg = dataclasses.replace(cfg, spp_ref=args.dn_eval_ref_spp)
-    eval_scs, _, _, eval_refs = D.make_dataset(eval_cfg, eval_seeds, torch)
     data_s = time.perf_counter() - t0
     den = native.Denoiser(seed=cfg.seed)
     t0 = time.perf_counter()
@@ -571,8 +571,9 @@ def run_denoise(args):
     calib = [D.plain_curve(cfg, sc, calib_refs[i], train_seeds[i], torch, spps=(4, 8, 16, 32, 64, 128, 256))
              for i, sc in enumerate(calib_scs)]
     fb_spp = D.fallback_spp_from(calib, cfg.target)
-    res = D.evaluate(cfg, den, {s: (sc, eval_refs[i]) for i, (s, sc) in enumerate(zip(eval_seeds, eval_scs))},
-                     torch, fb_spp)
+    t0 = time.perf_counter()
+    res = D.evaluate(cfg, den, D.iter_rooms(eval_cfg, eval_seeds, torch), torch, fb_spp)
+    eval_s = time.perf_counter() - t0
     rows = res["rooms"]
     tp = [r["time_plain_s"] for r in rows if r["spp_plain_to_target"] is not None]
     td = [r["time_final_s"] for r in rows]
@@ -595,7 +596,9 @@ def run_denoise(args):
             "inference_mean_s": float(np.mean([r["inference_s"] for r in rows])),
             "spp_plain_to_target": [r["spp_plain_to_target"] for r in rows],
             "loss_first_last": [losses[0][1], losses[-1][1]], "data_s": round(data_s, 1),
-            "train_s": round(train_s, 1)}
+            "train_s": round(train_s, 1), "eval_s": round(eval_s, 1),
+            "per_room": [{k: r[k] for k in ("seed", "relmse_noisy", "relmse_denoised", "relmse_final", "fallback",
+                                            "spp_plain_to_target", "time_plain_s", "time_final_s")} for r in rows]}
     print(json.dumps(line), flush=True)
 
 

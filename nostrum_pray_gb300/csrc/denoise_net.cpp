@@ -83,12 +83,23 @@ cudaError_t Denoiser::init(uint64_t seed) {
         tc_off_[i] = tc_total;
         tc_total += dn::tc_packed_weight_elems(pad16(convs_[i].cin), convs_[i].cout);
     }
+    // backward-data weights: the first convolution's input needs no gradient
+    size_t tcb_total = 0;
+    tcb_off_.assign(kNumConvs, 0);
+    for (int i = 1; i < kNumConvs; i++) {
+        tcb_off_[i] = tcb_total;
+        tcb_total += dn::tc_packed_weight_elems(pad16(convs_[i].cout), convs_[i].cin);
+    }
     plans_.assign(kNumConvs, dn::TcConvPlan{});
+    plans_bwd_.assign(kNumConvs, dn::TcConvPlan{});
+    plans_wg_.assign(kNumConvs, dn::TcWgradPlan{});
     cudaError_t e;
     if ((e = cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) return e;
     if ((e = take(w_, total)) != cudaSuccess || (e = take(g_, total)) != cudaSuccess ||
         (e = take(m_, total)) != cudaSuccess || (e = take(v_, total)) != cudaSuccess ||
         (e = take(wb_, total)) != cudaSuccess || (e = take(wtc_, tc_total)) != cudaSuccess ||
+        (e = take(wtcb_, tcb_total)) != cudaSuccess || (e = take(zero_bias_, 256)) != cudaSuccess ||
+        (e = cudaMemset(zero_bias_, 0, 256 * sizeof(float))) != cudaSuccess ||
         (e = take(loss_, 1)) != cudaSuccess || (e = take(err_, 1)) != cudaSuccess ||
         (e = cudaMemset(err_, 0, sizeof(int))) != cudaSuccess)
         return e;
@@ -118,6 +129,8 @@ cudaError_t Denoiser::refresh_tc_weights(cudaStream_t st) {
         const Conv &c = convs_[i];
         cudaError_t e = dn::tc_pack_weights(w_ + c.offset, wtc_ + tc_off_[i], c.cin, pad16(c.cin), c.cout, st);
         if (e != cudaSuccess) return e;
+        if (i > 0 && (e = dn::tc_pack_weights_bwd(w_ + c.offset, wtcb_ + tcb_off_[i], c.cin, c.cout, st)) != cudaSuccess)
+            return e;
     }
     return cudaSuccess;
 }
@@ -142,10 +155,14 @@ cudaError_t Denoiser::ensure(int n, int h, int w) {
     const size_t px = (size_t)n * h * w;
     if (px <= cap_pixels_ && h == h_ && w == w_dim_ && n == n_) return cudaSuccess;
     // keep the parameters, drop the activations
-    std::vector<void *> keep = {w_, g_, m_, v_, wb_, wtc_, loss_, err_};
+    std::vector<void *> keep = {w_, g_, m_, v_, wb_, wtc_, wtcb_, zero_bias_, loss_, err_};
     partial_ = nullptr;
     x16_ = nullptr;
+    gb16_ = nullptr;
+    partial_wg_ = nullptr;
     plans_.assign(kNumConvs, dn::TcConvPlan{});
+    plans_bwd_.assign(kNumConvs, dn::TcConvPlan{});
+    plans_wg_.assign(kNumConvs, dn::TcWgradPlan{});
     for (void *p : owned_)
         if (std::find(keep.begin(), keep.end(), p) == keep.end()) cudaFree(p);
     owned_ = keep;
@@ -182,17 +199,27 @@ cudaError_t Denoiser::ensure(int n, int h, int w) {
         if ((e = act(l, kEnc[l], true)) != cudaSuccess) return e;
     }
     if ((e = take(out_, px * 3)) != cudaSuccess || (e = take(gout_, px * 3)) != cudaSuccess ||
-        (e = take(gtmp_, px * 128)) != cudaSuccess || (e = take(x16_, px * pad16(kConvs[0][0]))) != cudaSuccess)
+        (e = take(gtmp_, px * 128)) != cudaSuccess || (e = take(x16_, px * pad16(kConvs[0][0]))) != cudaSuccess ||
+        (e = take(gb16_, px * 128)) != cudaSuccess)
         return e;
-    // split-tap partial sums of the tensor-core kernel: the largest need of any convolution
-    size_t partial = 0;
+    // split-tap partial sums of the tensor-core kernel: the largest need of
+    // any forward or backward-data convolution; per-group weight-gradient sums
+    size_t partial = 0, partial_wg = 0;
     for (int i = 0; i < kNumConvs; i++) {
         dn::TcConvPlan shape;
         const int l = kLevel[i];
         if (dn::tc_conv_plan(shape, act_[0].x, n, h >> l, w >> l, pad16(kConvs[i][0]), kConvs[i][1], true,
                              sm_count_) == cudaSuccess)
             partial = std::max(partial, shape.partial_floats);
+        if (i > 0 && dn::tc_conv_plan(shape, act_[0].x, n, h >> l, w >> l, pad16(kConvs[i][1]), kConvs[i][0], false,
+                                      sm_count_) == cudaSuccess)
+            partial = std::max(partial, shape.partial_floats);
+        dn::TcWgradPlan wg;
+        if (dn::tc_wgrad_plan(wg, act_[0].x, n, h >> l, w >> l, kConvs[i][0], pad16(kConvs[i][0]), kConvs[i][1],
+                              sm_count_) == cudaSuccess)
+            partial_wg = std::max(partial_wg, wg.partial_floats);
     }
+    if (partial_wg && (e = take(partial_wg_, partial_wg)) != cudaSuccess) return e;
     if (partial && (e = take(partial_, partial)) != cudaSuccess) return e;
     cap_pixels_ = px;
     return cudaSuccess;
@@ -282,21 +309,54 @@ cudaError_t Denoiser::backward(const float *target, cudaStream_t st) {
     for (Buf &b : act_)
         if (b.g) chk(cudaMemsetAsync(b.g, 0, (size_t)n * (h >> b.level) * (w >> b.level) * b.c * 4, st));
     chk(dn::l1_loss(out_, target, feat_, gout_, loss_, px * 3, st));
-    auto conv_bwd = [&](int ci, Buf &in, const float *gpre, int level) {
+    // input gradient (when in.g) and weight / bias gradients of convolution ci;
+    // with the tensor cores the input gradient is a forward convolution of
+    // the output gradient (BF16) with the transposed, tap-mirrored weights
+    auto conv_bwd = [&](int ci, Buf &in, const float *gpre, int level, bool need_dx) {
         const Conv &c = convs_[ci];
-        chk(dn::conv3x3_backward(in.x, wb_ + c.offset, gpre, in.g, g_ + c.offset,
-                                 g_ + c.offset + (size_t)c.cout * 9 * c.cin, n, h >> level, w >> level, c.cin, c.cout,
-                                 st));
+        const int hh = h >> level, ww = w >> level;
+        const size_t p = (size_t)n * hh * ww;
+        float *dw = g_ + c.offset, *db = dw + (size_t)c.cout * 9 * c.cin;
+        if (!tensor_cores_) {
+            chk(dn::conv3x3_backward(in.x, wb_ + c.offset, gpre, need_dx ? in.g : nullptr, dw, db, n, hh, ww, c.cin,
+                                     c.cout, st));
+            return;
+        }
+        // the output gradient in BF16, the operand of both tensor-core kernels
+        chk(dn::grad_bf16(gpre, gb16_, p, c.cout, pad16(c.cout), st));
+        if (need_dx) {
+            dn::TcConvPlan &pl = plans_bwd_[ci];
+            if (pl.x != gb16_ || pl.n != n || pl.h != hh || pl.w != ww) {
+                cudaError_t pe = dn::tc_conv_plan(pl, gb16_, n, hh, ww, pad16(c.cout), c.cin, false, sm_count_);
+                if (pe != cudaSuccess) {
+                    pl.x = nullptr;
+                    chk(pe);
+                    return;
+                }
+            }
+            chk(dn::conv3x3_forward_tc(pl, wtcb_ + tcb_off_[ci], zero_bias_, nullptr, in.g, partial_, err_, st));
+        }
+        dn::TcWgradPlan &wg = plans_wg_[ci];
+        if (wg.g != gb16_ || wg.n != n || wg.h != hh || wg.w != ww) {
+            cudaError_t pe = dn::tc_wgrad_plan(wg, gb16_, n, hh, ww, c.cin, pad16(c.cin), c.cout, sm_count_);
+            if (pe != cudaSuccess) {
+                wg.g = nullptr;
+                chk(pe);
+                return;
+            }
+        }
+        chk(dn::conv3x3_wgrad_tc(wg, plans_[ci], dw, partial_wg_, err_, st));
+        chk(dn::bias_grad(gpre, db, p, c.cout, st));
     };
     // output conv: input d0 (26)
-    conv_bwd(18, act_[26], gout_, 0);
+    conv_bwd(18, act_[26], gout_, 0, true);
     // layer tensor i was produced by conv j from tensor i-1 (within a level)
     // backward through (conv j: i-1 -> i) with the ReLU mask on i's gradient
     auto through = [&](int ci, int out_idx) {
         Buf &o = act_[out_idx];
         const size_t p = (size_t)n * (h >> o.level) * (w >> o.level);
         chk(dn::relu_mask(o.x, o.g, gtmp_, p * o.c, st));
-        conv_bwd(ci, act_[out_idx - 1], gtmp_, o.level);
+        conv_bwd(ci, act_[out_idx - 1], gtmp_, o.level, true);
     };
     const int skip_idx[4] = {11, 8, 5, 2};
     // decoder, deepest last in forward => first here: d0 (convs 16,17), d1 (14,15), d2 (12,13), d3 (10,11)
@@ -322,9 +382,7 @@ cudaError_t Denoiser::backward(const float *target, cudaStream_t st) {
             Buf &o = act_[1];
             const size_t p = (size_t)n * h * w;
             chk(dn::relu_mask(o.x, o.g, gtmp_, p * o.c, st));
-            const Conv &c = convs_[0];
-            chk(dn::conv3x3_backward(act_[0].x, wb_ + c.offset, gtmp_, nullptr, g_ + c.offset,
-                                     g_ + c.offset + (size_t)c.cout * 9 * c.cin, n, h, w, c.cin, c.cout, st));
+            conv_bwd(0, act_[0], gtmp_, 0, false);
         } else {
             through(2 * l, b_idx - 1);
             // pooled tensor (b_idx - 2) came from the previous level's output

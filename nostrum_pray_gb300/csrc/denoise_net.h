@@ -33,8 +33,8 @@ class Denoiser {
     // kernel choice as the previous one replays them from a CUDA graph
     cudaError_t denoise(const float *rad, const __half *feat, int n, int h, int w, float *out, cudaStream_t st);
     const float *loss_device() const { return loss_; }
-    // forward convolutions on the tcgen05 tensor cores (default) or on the
-    // CUDA cores
+    // forward and backward-data convolutions on the tcgen05 tensor cores
+    // (default) or on the CUDA cores
     void set_tensor_cores(bool on) { tensor_cores_ = on; }
     bool tensor_cores() const { return tensor_cores_; }
     // synchronises; false if a tensor-core kernel reported a timed-out wait
@@ -75,6 +75,16 @@ class Denoiser {
     float *partial_ = nullptr;
     std::vector<dn::TcConvPlan> plans_;
     int sm_count_ = 0;
+    // tensor-core backward-data: per convolution the transposed, tap-mirrored
+    // packed weights (dn::tc_pack_weights_bwd) and a plan over the output
+    // gradient in BF16 (gb16_), and a zero bias
+    __nv_bfloat16 *wtcb_ = nullptr, *gb16_ = nullptr;
+    std::vector<size_t> tcb_off_;
+    std::vector<dn::TcConvPlan> plans_bwd_;
+    float *zero_bias_ = nullptr;
+    // tensor-core weight gradients: one plan per convolution, per-group partial sums
+    std::vector<dn::TcWgradPlan> plans_wg_;
+    float *partial_wg_ = nullptr;
     float *out_ = nullptr, *gout_ = nullptr, *gtmp_ = nullptr;
     const __half *feat_ = nullptr;  // features of the last forward (the caller's buffer; used until the call returns)
     int *err_ = nullptr;

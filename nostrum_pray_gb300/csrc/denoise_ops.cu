@@ -179,6 +179,15 @@ __global__ void k_relu_mask(const __nv_bfloat16 *y, const float *g, float *out, 
     for (size_t i = gtid(); i < n; i += gstride()) out[i] = bf(y[i]) > 0.f ? g[i] : 0.f;
 }
 
+__global__ void k_grad_bf16(const float *g, __nv_bfloat16 *out, size_t pixels, int c, int c_pad) {
+    const size_t n = pixels * (size_t)c_pad;
+    for (size_t i = gtid(); i < n; i += gstride()) {
+        const size_t p = i / (size_t)c_pad;
+        const int k = (int)(i - p * c_pad);
+        out[i] = __float2bfloat16(k < c ? g[p * c + k] : 0.f);
+    }
+}
+
 __global__ void k_bias_grad(const float *g, float *db, size_t pixels, int c) {
     // one block per channel
     __shared__ float sm[256];
@@ -369,6 +378,15 @@ cudaError_t conv3x3_backward(const __nv_bfloat16 *x, const __nv_bfloat16 *w, con
 
 cudaError_t relu_mask(const __nv_bfloat16 *y, const float *g, float *out, size_t n, cudaStream_t st) {
     k_relu_mask<<<blocks_for(n), 256, 0, st>>>(y, g, out, n);
+    return cudaGetLastError();
+}
+cudaError_t bias_grad(const float *g, float *db, size_t pixels, int c, cudaStream_t st) {
+    k_bias_grad<<<c, 256, 0, st>>>(g, db, pixels, c);
+    return cudaGetLastError();
+}
+cudaError_t grad_bf16(const float *g, __nv_bfloat16 *out, size_t pixels, int c, int c_pad, cudaStream_t st) {
+    if (c_pad < c) return cudaErrorInvalidValue;
+    k_grad_bf16<<<blocks_for(pixels * (size_t)c_pad), 256, 0, st>>>(g, out, pixels, c, c_pad);
     return cudaGetLastError();
 }
 cudaError_t avgpool(const __nv_bfloat16 *x, __nv_bfloat16 *y, int n, int h, int w, int c, cudaStream_t st) {

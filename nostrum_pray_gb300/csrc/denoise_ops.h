@@ -33,14 +33,44 @@ cudaError_t tc_conv_plan(TcConvPlan &p, const __nv_bfloat16 *x, int n, int h, in
                          int sm_count);
 size_t tc_packed_weight_elems(int cin_pad, int cout);
 cudaError_t tc_pack_weights(const float *w, __nv_bfloat16 *packed, int cin, int cin_pad, int cout, cudaStream_t st);
+// Weights of the backward-data convolution of a forward convolution with
+// cin_f inputs and cout_f outputs (w[cout_f][9][cin_f]): a plan with
+// cin = cout_f rounded up to 16 and cout = cin_f runs it on the output
+// gradient (as BF16, grad_bf16) and writes the input gradient.
+cudaError_t tc_pack_weights_bwd(const float *w, __nv_bfloat16 *packed, int cin_f, int cout_f, cudaStream_t st);
 cudaError_t conv3x3_forward_tc(const TcConvPlan &p, const __nv_bfloat16 *wpacked, const float *bias,
                                __nv_bfloat16 *y, float *y32, float *partial, int *err, cudaStream_t st);
+// Weight gradient of a 3x3 convolution on the tensor cores:
+// dw[co][tap][ci] += sum over pixels p of g[p][co] * x[p + offset(tap)][ci],
+// a GEMM with M = output channels (padded to 128), N = input channels, K =
+// pixels. g: the output gradient as BF16 with cout_pad = cout rounded up to
+// 16 channels (grad_bf16); x: the convolution's input, read through the
+// forward plan's halo tensor map (fwd: a plan over x with cin = cin_pad).
+// Each CTA accumulates the nine taps (or a group of them, as many as tensor
+// memory holds) over a group of 16 x 8 tiles and writes them to `partial`
+// (partial_floats floats); a second kernel adds the groups in order into dw.
+struct TcWgradPlan {
+    alignas(64) unsigned char gmap[128];  // CUtensorMap of g: (cout_pad, W, H, N), box (8, 8, 16, 1)
+    const __nv_bfloat16 *g;
+    int n, h, w, cin, cin_pad, cout, cout_pad;
+    int tiles_x, tiles_y, tiles, tiles_per_cta, groups, taps_per_pass, passes, tmem_cols;
+    uint32_t b_off, bar_off;
+    size_t smem, partial_floats;
+};
+cudaError_t tc_wgrad_plan(TcWgradPlan &p, const __nv_bfloat16 *g, int n, int h, int w, int cin, int cin_pad, int cout,
+                          int sm_count);
+cudaError_t conv3x3_wgrad_tc(const TcWgradPlan &p, const TcConvPlan &fwd, float *dw, float *partial, int *err,
+                             cudaStream_t st);
 cudaError_t conv3x3_forward(const __nv_bfloat16 *x, const __nv_bfloat16 *w, const float *b, __nv_bfloat16 *y,
                             float *y32, int n, int h, int wd, int cin, int cout, bool relu, cudaStream_t st);
 // gpre: output gradient after the ReLU mask (FP32, n*h*w*cout); dx may be NULL
 cudaError_t conv3x3_backward(const __nv_bfloat16 *x, const __nv_bfloat16 *w, const float *gpre, float *dx, float *dw,
                              float *db, int n, int h, int wd, int cin, int cout, cudaStream_t st);
 cudaError_t relu_mask(const __nv_bfloat16 *y, const float *g, float *out, size_t n, cudaStream_t st);
+// db[c] += sum over pixels of g[p][c]
+cudaError_t bias_grad(const float *g, float *db, size_t pixels, int c, cudaStream_t st);
+// g (pixels x c FP32) as BF16 with c_pad >= c channels (the pad zero)
+cudaError_t grad_bf16(const float *g, __nv_bfloat16 *out, size_t pixels, int c, int c_pad, cudaStream_t st);
 cudaError_t avgpool(const __nv_bfloat16 *x, __nv_bfloat16 *y, int n, int h, int w, int c, cudaStream_t st);
 cudaError_t avgpool_backward(const float *gy, float *gx, int n, int h, int w, int c, cudaStream_t st);
 cudaError_t upsample_backward(const float *gy, float *gx, int n, int h, int w, int c, int cy, cudaStream_t st);

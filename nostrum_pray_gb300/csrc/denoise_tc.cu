@@ -468,6 +468,184 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_tc_persistent(const __grid_
 
 // Sum of the split partials in split order, plus bias, ReLU, store; four
 // channels per thread when cout is a multiple of 4, else one.
+// ---- weight gradient ---------------------------------------------------------
+//
+// dw[co][tap][ci] = sum_p g[p][co] x[p + offset(tap)][ci]: per tap a GEMM with
+// M = co (128 rows: the output-gradient channels, zero rows above cout),
+// N = ci (cin_pad), K = pixels. Both operands come straight from the
+// channel-planar tiles TMA writes ([8-channel plane][pixel][8 channels], 16
+// bytes per pixel), read as MN-major matrices (the 8 channels of a pixel
+// contiguous, pixels along K):
+//   A: the tile's output gradient, one 2,048-byte plane per 8 channels
+//      (16 x 8 pixels); core matrices 128 bytes apart along K (8 pixels = one
+//      tile row) and one plane apart along M;
+//   B: the input halo (18 x 10 pixels per plane, as in the forward pass);
+//      for tap (dy, dx) the K-step covering tile rows 2k and 2k + 1 starts at
+//      halo pixel (2k + dy, dx), core matrices one halo row (160 bytes) apart
+//      along K and one plane apart along N.
+// So every tap reads the same halo, shifted by whole 16-byte pixels, as in
+// the forward pass. Each CTA owns a group of tiles and a group of taps
+// (tensor memory holds taps_per_pass x cin_pad FP32 columns), loads a tile's
+// planes, issues its MMAs, and waits for them before loading the next tile.
+// The accumulators go to partial[group][tap][co][ci]; k_wgrad_finalize adds
+// the groups in order into dw. Every wait is bounded (error flag, drain,
+// TMEM freed).
+constexpr uint32_t kGradPlaneBytes = kTileW * kTileH * 16;  // 2,048
+constexpr int kGradPlanes = 16;                             // 128 rows of A
+
+struct WgArgs {
+    float *partial;  // [group][9][128][cin_pad]
+    int n, h, wd, cin_pad, cout_pad;
+    int tiles_x, tiles_y, tiles, tiles_per_cta, taps_per_pass, tmem_cols;
+    uint32_t b_off, bar_off;
+    int *err;
+};
+
+// MN-major A and B: transpose bits of the kind::f16 instruction descriptor
+__host__ __device__ constexpr uint32_t inst_desc_mn(int m, int n) { return inst_desc(m, n) | (1u << 15) | (1u << 16); }
+
+// One plane (8 channels) of a tile of the output gradient: box (8, 8, 16, 1).
+__device__ __forceinline__ void tma_tile(uint32_t dst, const CUtensorMap *map, uint32_t bar, int c, int x, int y,
+                                         int img) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, "
+        "%6}], [%2];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c), "r"(x), "r"(y), "r"(img)
+        : "memory");
+}
+
+__global__ void __launch_bounds__(128) k_wgrad_tc(const __grid_constant__ CUtensorMap gmap,
+                                                  const __grid_constant__ CUtensorMap xmap, WgArgs P) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t abase = smem_u32(smem), bbase = abase + P.b_off;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + P.bar_off);  // [0] tile loaded, [1] MMAs done
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2);
+    int *okflag = reinterpret_cast<int *>(tmem_slot + 1);
+    const int gplanes = P.cout_pad >> 3, xplanes = P.cin_pad >> 3;
+    const int group = blockIdx.x, pass = blockIdx.y;
+    const int tap0 = pass * P.taps_per_pass, ntaps = min(9 - tap0, P.taps_per_pass);
+    const int t_begin = group * P.tiles_per_cta, t_end = min(P.tiles, t_begin + P.tiles_per_cta);
+
+    // the rows of A above cout_pad stay zero
+    for (uint32_t i = (uint32_t)gplanes * kGradPlaneBytes / 16 + tid; i < kGradPlanes * kGradPlaneBytes / 16; i += 128)
+        reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0u, 0u, 0u, 0u);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(P.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        mbar_init(smem_u32(&bars[0]));
+        mbar_init(smem_u32(&bars[1]));
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the zero rows, for the tensor cores
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (tid == 0) {
+        bool ok = true;
+        const uint32_t idesc = inst_desc_mn(128, P.cin_pad);
+        const uint32_t bytes = (uint32_t)gplanes * kGradPlaneBytes + (uint32_t)xplanes * kChunkBytes;
+        const int per_img = P.tiles_x * P.tiles_y;
+        uint32_t phase = 0;
+        bool first = true;
+        for (int t = t_begin; t < t_end && ok; t++, phase ^= 1u) {
+            const int img = t / per_img, rem = t - img * per_img;
+            const int y0 = (rem / P.tiles_x) * kTileH, x0 = (rem % P.tiles_x) * kTileW;
+            // the previous tile's MMAs read these buffers: they completed (bars[1]) before this load
+            mbar_expect_tx(smem_u32(&bars[0]), bytes);
+            for (int c = 0; c < gplanes; c++)
+                tma_tile(abase + c * kGradPlaneBytes, &gmap, smem_u32(&bars[0]), 8 * c, x0, y0, img);
+            for (int c = 0; c < xplanes; c++)
+                tma_halo(bbase + c * kPlaneBytes, &xmap, smem_u32(&bars[0]), 8 * c, x0 - 1, y0 - 1, img);
+            if (!mbar_wait(smem_u32(&bars[0]), phase)) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            for (int q = 0; q < ntaps; q++) {
+                const int tap = tap0 + q, dy = tap / 3, dx = tap - 3 * (tap / 3);
+                const uint32_t d = tmem + (uint32_t)(q * P.cin_pad);
+                for (int k = 0; k < kTileH / 2; k++) {
+                    const uint64_t ad = smem_desc(abase + (uint32_t)k * 256u, 128u, kGradPlaneBytes);
+                    const uint64_t bd =
+                        smem_desc(bbase + (uint32_t)((2 * k + dy) * kHaloW + dx) * 16u, kRowBytes, kPlaneBytes);
+                    mma(d, ad, bd, idesc, (first && k == 0) ? 0u : 1u);
+                }
+            }
+            first = false;
+            commit(smem_u32(&bars[1]));
+            if (!mbar_wait(smem_u32(&bars[1]), phase)) {
+                ok = false;
+                break;
+            }
+        }
+        *okflag = !ok ? 0 : (first ? 2 : 1);  // 2: no tile in this group
+        if (!ok) {
+            // bounded drain of what may still be in flight
+            mbar_wait(smem_u32(&bars[0]), phase);
+            commit(smem_u32(&bars[1]));
+            mbar_wait(smem_u32(&bars[1]), phase);
+        }
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int flag = *okflag;
+    if (flag == 0 && tid == 0) atomicExch(P.err, 1);
+    // epilogue: warp q reads TMEM lanes 32q..32q+31 (rows co), all columns
+    const int co = warp * 32 + (tid & 31);
+    for (int q = 0; q < ntaps; q++) {
+        float *dst = P.partial + (((size_t)group * 9 + tap0 + q) * 128 + co) * P.cin_pad;
+        for (int c0 = 0; c0 < P.cin_pad; c0 += 16) {
+            uint32_t r[16];
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(q * P.cin_pad + c0);
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15])
+                : "r"(taddr)
+                : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            float4 *o = reinterpret_cast<float4 *>(dst + c0);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const float v0 = flag == 1 ? __uint_as_float(r[4 * k]) : 0.f;
+                const float v1 = flag == 1 ? __uint_as_float(r[4 * k + 1]) : 0.f;
+                const float v2 = flag == 1 ? __uint_as_float(r[4 * k + 2]) : 0.f;
+                const float v3 = flag == 1 ? __uint_as_float(r[4 * k + 3]) : 0.f;
+                o[k] = make_float4(v0, v1, v2, v3);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(P.tmem_cols)
+                     : "memory");
+    }
+}
+
+// dw[co][tap][ci] += sum over groups (in order) of partial[group][tap][co][ci]
+__global__ void k_wgrad_finalize(const float *partial, float *dw, int groups, int cout, int cin, int cin_pad) {
+    const size_t total = (size_t)cout * 9 * cin;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int ci = (int)(i % cin);
+        const size_t rest = i / cin;
+        const int tap = (int)(rest % 9), co = (int)(rest / 9);
+        float v = 0.f;
+        for (int g = 0; g < groups; g++) v += partial[(((size_t)g * 9 + tap) * 128 + co) * cin_pad + ci];
+        dw[i] += v;
+    }
+}
+
 template <int kVec>
 __global__ void k_conv_finalize(const float *partial, const float *bias, __nv_bfloat16 *y, float *y32, size_t M,
                                 int npad, int cout, int splits, int relu) {
@@ -522,6 +700,27 @@ __global__ void k_pack_weights(const float *w, __nv_bfloat16 *out, int cin, int 
     }
 }
 
+// The backward-data convolution's weights, packed like k_pack_weights: the
+// input gradient of a 3x3 convolution is a 3x3 convolution of the output
+// gradient (cout_f channels, padded to cin_pad) with the weights transposed
+// (output channel ci, input channel co) and the taps mirrored (tap 8 - t):
+// out[tap][chunk][ci][8] = w[co][8 - tap][ci], w[cout_f][9][cin_f].
+__global__ void k_pack_weights_bwd(const float *w, __nv_bfloat16 *out, int cin_f, int cout_f, int cin_pad,
+                                   int npad) {
+    const int nchunk = cin_pad >> 3;
+    const size_t total = (size_t)9 * cin_pad * npad;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int e = (int)(i & 7);
+        const size_t rowi = i >> 3;
+        const int r = (int)(rowi % npad);  // ci
+        const size_t ct = rowi / npad;
+        const int chunk = (int)(ct % nchunk), tap = (int)(ct / nchunk);
+        const int co = chunk * 8 + e;
+        const float v = (r < cin_f && co < cout_f) ? w[((size_t)co * 9 + (8 - tap)) * cin_f + r] : 0.f;
+        out[i] = __float2bfloat16(v);
+    }
+}
+
 unsigned grid_for(size_t n) {
     const size_t b = (n + 255) / 256;
     return (unsigned)(b < 4096 ? (b ? b : 1) : 4096);
@@ -552,6 +751,95 @@ cudaError_t tc_pack_weights(const float *w, __nv_bfloat16 *packed, int cin, int 
     const int npad = (cout + 15) / 16 * 16;
     k_pack_weights<<<grid_for(tc_packed_weight_elems(cin_pad, cout)), 256, 0, st>>>(w, packed, cin, cin_pad, cout,
                                                                                    npad);
+    return cudaGetLastError();
+}
+
+cudaError_t tc_pack_weights_bwd(const float *w, __nv_bfloat16 *packed, int cin_f, int cout_f, cudaStream_t st) {
+    const int cin_pad = (cout_f + 15) / 16 * 16, npad = (cin_f + 15) / 16 * 16;
+    k_pack_weights_bwd<<<grid_for(tc_packed_weight_elems(cin_pad, cin_f)), 256, 0, st>>>(w, packed, cin_f, cout_f,
+                                                                                        cin_pad, npad);
+    return cudaGetLastError();
+}
+
+cudaError_t tc_wgrad_plan(TcWgradPlan &p, const __nv_bfloat16 *g, int n, int h, int w, int cin, int cin_pad, int cout,
+                          int sm_count) {
+    std::memset(&p, 0, sizeof(p));
+    if (n <= 0 || h <= 0 || w <= 0 || cin <= 0 || cin > cin_pad || (cin_pad & 15) || cin_pad > 256 || cout <= 0 ||
+        cout > 128)
+        return cudaErrorInvalidValue;
+    p.g = g, p.n = n, p.h = h, p.w = w, p.cin = cin, p.cin_pad = cin_pad, p.cout = cout;
+    p.cout_pad = (cout + 15) / 16 * 16;
+    p.tiles_x = (w + kTileW - 1) / kTileW;
+    p.tiles_y = (h + kTileH - 1) / kTileH;
+    const long long tiles = (long long)n * p.tiles_x * p.tiles_y;
+    if (tiles > 0x7FFFFFFFLL) return cudaErrorInvalidValue;
+    p.tiles = (int)tiles;
+    // taps per pass: as many accumulators of cin_pad columns as 512 TMEM columns hold
+    p.taps_per_pass = 512 / cin_pad < 9 ? 512 / cin_pad : 9;
+    p.passes = (9 + p.taps_per_pass - 1) / p.taps_per_pass;
+    int cols = 32;
+    while (cols < p.taps_per_pass * cin_pad) cols <<= 1;
+    p.tmem_cols = cols;
+    // about two CTAs per SM over all groups and passes
+    const long long want = 2LL * sm_count;
+    long long per = (tiles * p.passes + want - 1) / want;
+    if (per < 1) per = 1;
+    p.tiles_per_cta = (int)per;
+    p.groups = (int)((tiles + per - 1) / per);
+    p.b_off = kGradPlanes * kGradPlaneBytes;
+    p.bar_off = (p.b_off + (uint32_t)(cin_pad / 8) * kPlaneBytes + 15) & ~15u;
+    p.smem = p.bar_off + 2 * 8 + 16;
+    if (p.smem > kSmemMax) return cudaErrorInvalidValue;
+    // no more CTAs per SM than TMEM has columns for (tcgen05.alloc would wait):
+    // ask for enough shared memory to keep the others off the SM
+    const size_t max_ctas = 512 / cols;
+    if (kSmemPerSm / (p.smem + 1024) > max_ctas) {
+        p.smem = kSmemPerSm / max_ctas - 1024 + 16;
+        if (p.smem > kSmemMax) p.smem = kSmemMax;
+    }
+    p.partial_floats = (size_t)p.groups * 9 * 128 * cin_pad;
+    EncodeTiled enc = encode_fn();
+    if (!enc) return cudaErrorNotSupported;
+    const cuuint64_t dims[4] = {(cuuint64_t)p.cout_pad, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
+    const cuuint64_t strides[3] = {(cuuint64_t)p.cout_pad * 2, (cuuint64_t)w * p.cout_pad * 2,
+                                   (cuuint64_t)h * w * p.cout_pad * 2};
+    const cuuint32_t box[4] = {8, kTileW, kTileH, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUtensorMap *map = reinterpret_cast<CUtensorMap *>(p.gmap);
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16 *>(g), dims, strides, box,
+                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+cudaError_t conv3x3_wgrad_tc(const TcWgradPlan &p, const TcConvPlan &fwd, float *dw, float *partial, int *err,
+                             cudaStream_t st) {
+    if (!partial || !dw || fwd.cin != p.cin_pad || fwd.n != p.n || fwd.h != p.h || fwd.w != p.w)
+        return cudaErrorInvalidValue;
+    static std::atomic<uint64_t> attr_set{0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t bit = dev < 64 ? 1ull << dev : 0;
+    if (!bit || !(attr_set.load() & bit)) {
+        e = cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax);
+        if (e != cudaSuccess) return e;
+        attr_set.fetch_or(bit);
+    }
+    WgArgs a;
+    a.partial = partial;
+    a.n = p.n, a.h = p.h, a.wd = p.w, a.cin_pad = p.cin_pad, a.cout_pad = p.cout_pad;
+    a.tiles_x = p.tiles_x, a.tiles_y = p.tiles_y, a.tiles = p.tiles, a.tiles_per_cta = p.tiles_per_cta;
+    a.taps_per_pass = p.taps_per_pass, a.tmem_cols = p.tmem_cols;
+    a.b_off = p.b_off, a.bar_off = p.bar_off;
+    a.err = err;
+    CUtensorMap gm, xm;
+    std::memcpy(&gm, p.gmap, sizeof(gm));
+    std::memcpy(&xm, fwd.tmap, sizeof(xm));
+    k_wgrad_tc<<<dim3((unsigned)p.groups, (unsigned)p.passes), 128, p.smem, st>>>(gm, xm, a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_wgrad_finalize<<<grid_for((size_t)p.cout * 9 * p.cin), 256, 0, st>>>(partial, dw, p.groups, p.cout, p.cin,
+                                                                          p.cin_pad);
     return cudaGetLastError();
 }
 
@@ -614,8 +902,11 @@ cudaError_t tc_conv_plan(TcConvPlan &p, const __nv_bfloat16 *x, int n, int h, in
     p.tmem_cols = cols;
     // no more CTAs per SM than TMEM has columns for (tcgen05.alloc would wait)
     const size_t max_ctas = 512 / cols;
-    if (kSmemPerSm / (smem + 1024) > max_ctas) smem = kSmemPerSm / max_ctas - 1024 + 16;
     if (smem > kSmemMax) return cudaErrorInvalidValue;
+    if (kSmemPerSm / (smem + 1024) > max_ctas) {
+        smem = kSmemPerSm / max_ctas - 1024 + 16;
+        if (smem > kSmemMax) smem = kSmemMax;  // one CTA per SM
+    }
     p.smem = smem;
     if (p.persistent) {
         size_t per_sm = kSmemPerSm / (smem + 1024);

@@ -123,15 +123,34 @@ def relmse(img, ref, torch) -> float:
     return float(out.item())
 
 
-def make_dataset(cfg: DenoiseConfig, seeds: List[int], torch, res: Optional[int] = None):
+def make_dataset(cfg: DenoiseConfig, seeds: List[int], torch, res: Optional[int] = None, keep_scenes: bool = True):
+    """(scenes, noisy radiance, features, references) stacked over `seeds`;
+    with keep_scenes False each scene is closed once rendered (its device
+    memory, including the path tracer's scratch, is released) and the scene
+    list is empty."""
     rads, feats, refs, scs = [], [], [], []
     for s in seeds:
         sc, rad, feat, ref = render_room(cfg, s, torch, res)
         rads.append(rad)
         feats.append(feat)
-        refs.append(ref)
-        scs.append(sc)
+        refs.append(ref.to(torch.float32) if not keep_scenes else ref)
+        if keep_scenes:
+            scs.append(sc)
+        else:
+            sc.close()
     return scs, torch.stack(rads), torch.stack(feats), torch.stack(refs)
+
+
+def iter_rooms(cfg: DenoiseConfig, seeds: List[int], torch):
+    """(seed, scene, FP64 reference) for each seed, rendered when reached; the
+    scene is closed when the caller moves on, so only one room's device memory
+    is held at a time."""
+    for s in seeds:
+        sc, _, _, ref = render_room(cfg, s, torch)
+        try:
+            yield s, sc, ref
+        finally:
+            sc.close()
 
 
 def train(den: native.Denoiser, rad, feat, ref, cfg: DenoiseConfig, torch, log_every: int = 100):
@@ -259,8 +278,11 @@ def denoised_eval(cfg: DenoiseConfig, den, sc, ref, room_seed: int, torch):
 
 
 def evaluate(cfg: DenoiseConfig, den, eval_rooms, torch, fallback_spp: int) -> Dict:
+    """eval_rooms: a dict seed -> (scene, reference), or an iterable of
+    (seed, scene, reference) such as iter_rooms."""
     rows = []
-    for seed, (sc, ref) in eval_rooms.items():
+    items = ((s, sc, ref) for s, (sc, ref) in eval_rooms.items()) if isinstance(eval_rooms, dict) else eval_rooms
+    for seed, sc, ref in items:
         curve = plain_curve(cfg, sc, ref, seed, torch, spps=(1, 2, 4, 8, 16, 32, 64, 128, 256))
         plain = plain_to_target(cfg, sc, ref, seed, torch, curve)
         d = denoised_eval(cfg, den, sc, ref, seed, torch)
