@@ -41,8 +41,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["icosphere", "soup", "room", "batch", "cornell", "denoise", "denoise-infer"],
-                    default="icosphere")
+    ap.add_argument("--workload", choices=["icosphere", "soup", "room", "batch", "cornell", "denoise", "denoise-infer",
+                                           "denoise-train"], default="icosphere")
     ap.add_argument("--dn-steps", type=int, default=1000, help="denoise: training steps")
     ap.add_argument("--dn-train", type=int, default=96, help="denoise: training rooms")
     ap.add_argument("--dn-eval", type=int, default=16, help="denoise: held-out rooms")
@@ -664,6 +664,51 @@ def run_denoise_infer(args):
     print(json.dumps(line), flush=True)
 
 
+def run_denoise_train(args):
+    """Denoiser training steps (forward, L1 loss, backward, Adam) on a fixed
+    random batch of 8 crops of 128 x 128, the training shape of the denoise
+    workload, on the tensor cores (--dn-cuda-cores: every convolution on the
+    CUDA cores)."""
+    import torch
+    from nostrum_pray_gb300 import denoise as D, native
+    torch.cuda.set_device(0)
+    n, h, w = 8, 128, 128
+    rng = np.random.default_rng(0)
+    rad = torch.from_numpy((rng.random((n, h, w, 3)) * 2).astype(np.float32)).cuda()
+    feat = torch.from_numpy(rng.random((n, h, w, 7)).astype(np.float16)).cuda()
+    tgt = torch.from_numpy(rng.random((n, h, w, 3)).astype(np.float32)).cuda()
+    den = native.Denoiser(seed=1)
+    if args.dn_cuda_cores:
+        den.set_tensor_cores(False)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    clocks = ClockSampler(0)
+    clocks.start()
+    ms = _timed_frames(lambda: den.train_step(rad, feat, tgt, 1e-4), args.steps, args.warmup, flush)
+    clk = clocks.stop()
+    den.check()
+    # forward, backward-data (every convolution but the first) and weight gradient: 2 FLOPs per MAC each
+    fwd = D.forward_flops(h, w, n)
+    first = 2 * 9 * D.CONVS[0][0] * D.CONVS[0][1] * h * w * n
+    flops = 3 * fwd - first
+    per = ms / args.steps / 1e3
+    peak, peak_kind = measured_bf16()
+    achieved = flops / per / 1e12
+    line = {"metric": "training steps/s", "value": round(args.steps / (ms / 1e3), 2), "unit": "steps/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": f"U-Net denoiser training step (forward, L1 loss, backward, Adam; {D.num_params()} "
+                                   f"parameters), batch {n} x {h}x{w}, random inputs",
+                       "tensor_cores": not args.dn_cuda_cores, "l2": "flushed between steps"},
+            "roofline": {"bound": "tensor", "achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s",
+                         "frac": round(achieved / peak, 5), "traffic": None, "peak_kind": peak_kind,
+                         "algorithmic_flops_per_step": flops,
+                         "note": "convolution FLOPs of the forward pass, the backward-data pass (all but the first "
+                                 "convolution) and the weight gradients over the whole step's time (pooling, "
+                                 "upsampling, loss, Adam and format kernels included)"},
+            "clocks": clk}
+    return line
+
+
 def main():
     args = parse()
     if args.impl == "reference" and args.workload == "cornell":
@@ -680,6 +725,8 @@ def main():
         run_denoise(args)
     elif args.workload == "denoise-infer":
         run_denoise_infer(args)
+    elif args.workload == "denoise-train":
+        print(json.dumps(run_denoise_train(args)), flush=True)
     else:
         run_ours(args)
 
