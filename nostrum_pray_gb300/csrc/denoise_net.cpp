@@ -120,19 +120,36 @@ cudaError_t Denoiser::init(uint64_t seed) {
         (e = cudaMemcpy(v_, zeros.data(), total * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
         return e;
     step_ = 0;
+    // the packing jobs: each convolution's forward weights, then its
+    // backward-data weights (all but the first)
+    std::vector<dn::TcPackJob> jobs;
+    size_t begin = 0;
+    for (int i = 0; i < kNumConvs; i++) {
+        const Conv &c = convs_[i];
+        for (int bwd = 0; bwd < (i > 0 ? 2 : 1); bwd++) {
+            dn::TcPackJob j;
+            j.w = w_ + c.offset;
+            j.out = bwd ? wtcb_ + tcb_off_[i] : wtc_ + tc_off_[i];
+            j.begin = begin;
+            j.cin_f = c.cin, j.cout_f = c.cout, j.bwd = bwd;
+            j.cin_pad = bwd ? pad16(c.cout) : pad16(c.cin);
+            j.npad = bwd ? pad16(c.cin) : pad16(c.cout);
+            begin += (size_t)9 * j.cin_pad * j.npad;
+            jobs.push_back(j);
+        }
+    }
+    n_pack_jobs_ = (int)jobs.size();
+    pack_total_ = begin;
+    if ((e = take(pack_jobs_, jobs.size())) != cudaSuccess ||
+        (e = cudaMemcpy(pack_jobs_, jobs.data(), jobs.size() * sizeof(dn::TcPackJob), cudaMemcpyHostToDevice)) !=
+            cudaSuccess)
+        return e;
     if ((e = dn::to_bf16(w_, wb_, total, 0)) != cudaSuccess) return e;
     return refresh_tc_weights(0);
 }
 
 cudaError_t Denoiser::refresh_tc_weights(cudaStream_t st) {
-    for (int i = 0; i < kNumConvs; i++) {
-        const Conv &c = convs_[i];
-        cudaError_t e = dn::tc_pack_weights(w_ + c.offset, wtc_ + tc_off_[i], c.cin, pad16(c.cin), c.cout, st);
-        if (e != cudaSuccess) return e;
-        if (i > 0 && (e = dn::tc_pack_weights_bwd(w_ + c.offset, wtcb_ + tcb_off_[i], c.cin, c.cout, st)) != cudaSuccess)
-            return e;
-    }
-    return cudaSuccess;
+    return dn::tc_pack_all(pack_jobs_, n_pack_jobs_, pack_total_, st);
 }
 
 cudaError_t Denoiser::set_params(const float *host) {
@@ -155,10 +172,11 @@ cudaError_t Denoiser::ensure(int n, int h, int w) {
     const size_t px = (size_t)n * h * w;
     if (px <= cap_pixels_ && h == h_ && w == w_dim_ && n == n_) return cudaSuccess;
     // keep the parameters, drop the activations
-    std::vector<void *> keep = {w_, g_, m_, v_, wb_, wtc_, wtcb_, zero_bias_, loss_, err_};
+    std::vector<void *> keep = {w_, g_, m_, v_, wb_, wtc_, wtcb_, zero_bias_, pack_jobs_, loss_, err_};
     partial_ = nullptr;
     x16_ = nullptr;
     gb16_ = nullptr;
+    bias_part_ = nullptr;
     partial_wg_ = nullptr;
     plans_.assign(kNumConvs, dn::TcConvPlan{});
     plans_bwd_.assign(kNumConvs, dn::TcConvPlan{});
@@ -200,7 +218,8 @@ cudaError_t Denoiser::ensure(int n, int h, int w) {
     }
     if ((e = take(out_, px * 3)) != cudaSuccess || (e = take(gout_, px * 3)) != cudaSuccess ||
         (e = take(gtmp_, px * 128)) != cudaSuccess || (e = take(x16_, px * pad16(kConvs[0][0]))) != cudaSuccess ||
-        (e = take(gb16_, px * 128)) != cudaSuccess)
+        (e = take(gb16_, px * 128)) != cudaSuccess ||
+        (e = take(bias_part_, (size_t)dn::kGradPrepBlocks * 128)) != cudaSuccess)
         return e;
     // split-tap partial sums of the tensor-core kernel: the largest need of
     // any forward or backward-data convolution; per-group weight-gradient sums
@@ -309,21 +328,28 @@ cudaError_t Denoiser::backward(const float *target, cudaStream_t st) {
     for (Buf &b : act_)
         if (b.g) chk(cudaMemsetAsync(b.g, 0, (size_t)n * (h >> b.level) * (w >> b.level) * b.c * 4, st));
     chk(dn::l1_loss(out_, target, feat_, gout_, loss_, px * 3, st));
-    // input gradient (when in.g) and weight / bias gradients of convolution ci;
-    // with the tensor cores the input gradient is a forward convolution of
-    // the output gradient (BF16) with the transposed, tap-mirrored weights
-    auto conv_bwd = [&](int ci, Buf &in, const float *gpre, int level, bool need_dx) {
+    // input gradient (when need_dx) and weight / bias gradients of convolution
+    // ci from its output gradient g, masked by the ReLU of its output y (NULL:
+    // no ReLU). With the tensor cores the input gradient is a forward
+    // convolution of the masked gradient (BF16) with the transposed,
+    // tap-mirrored weights, and one pass over g gives that BF16 operand and
+    // the bias gradient.
+    auto conv_bwd = [&](int ci, Buf &in, const float *g, const __nv_bfloat16 *y, int level, bool need_dx) {
         const Conv &c = convs_[ci];
         const int hh = h >> level, ww = w >> level;
         const size_t p = (size_t)n * hh * ww;
         float *dw = g_ + c.offset, *db = dw + (size_t)c.cout * 9 * c.cin;
         if (!tensor_cores_) {
+            const float *gpre = g;
+            if (y) {
+                chk(dn::relu_mask(y, g, gtmp_, p * c.cout, st));
+                gpre = gtmp_;
+            }
             chk(dn::conv3x3_backward(in.x, wb_ + c.offset, gpre, need_dx ? in.g : nullptr, dw, db, n, hh, ww, c.cin,
                                      c.cout, st));
             return;
         }
-        // the output gradient in BF16, the operand of both tensor-core kernels
-        chk(dn::grad_bf16(gpre, gb16_, p, c.cout, pad16(c.cout), st));
+        chk(dn::grad_prep(y, g, gb16_, bias_part_, db, p, c.cout, pad16(c.cout), st));
         if (need_dx) {
             dn::TcConvPlan &pl = plans_bwd_[ci];
             if (pl.x != gb16_ || pl.n != n || pl.h != hh || pl.w != ww) {
@@ -346,17 +372,14 @@ cudaError_t Denoiser::backward(const float *target, cudaStream_t st) {
             }
         }
         chk(dn::conv3x3_wgrad_tc(wg, plans_[ci], dw, partial_wg_, err_, st));
-        chk(dn::bias_grad(gpre, db, p, c.cout, st));
     };
-    // output conv: input d0 (26)
-    conv_bwd(18, act_[26], gout_, 0, true);
+    // output conv: input d0 (26), no ReLU
+    conv_bwd(18, act_[26], gout_, nullptr, 0, true);
     // layer tensor i was produced by conv j from tensor i-1 (within a level)
     // backward through (conv j: i-1 -> i) with the ReLU mask on i's gradient
     auto through = [&](int ci, int out_idx) {
         Buf &o = act_[out_idx];
-        const size_t p = (size_t)n * (h >> o.level) * (w >> o.level);
-        chk(dn::relu_mask(o.x, o.g, gtmp_, p * o.c, st));
-        conv_bwd(ci, act_[out_idx - 1], gtmp_, o.level, true);
+        conv_bwd(ci, act_[out_idx - 1], o.g, o.x, o.level, true);
     };
     const int skip_idx[4] = {11, 8, 5, 2};
     // decoder, deepest last in forward => first here: d0 (convs 16,17), d1 (14,15), d2 (12,13), d3 (10,11)
@@ -379,10 +402,7 @@ cudaError_t Denoiser::backward(const float *target, cudaStream_t st) {
         through(2 * l + 1, b_idx);
         if (l == 0) {
             // first conv's input is x0 (no gradient needed): weights only
-            Buf &o = act_[1];
-            const size_t p = (size_t)n * h * w;
-            chk(dn::relu_mask(o.x, o.g, gtmp_, p * o.c, st));
-            conv_bwd(0, act_[0], gtmp_, 0, false);
+            conv_bwd(0, act_[0], act_[1].g, act_[1].x, 0, false);
         } else {
             through(2 * l, b_idx - 1);
             // pooled tensor (b_idx - 2) came from the previous level's output

@@ -82,9 +82,14 @@ class Denoiser {
     std::vector<size_t> tcb_off_;
     std::vector<dn::TcConvPlan> plans_bwd_;
     float *zero_bias_ = nullptr;
+    // every forward and backward-data packing as one launch (dn::tc_pack_all)
+    dn::TcPackJob *pack_jobs_ = nullptr;
+    int n_pack_jobs_ = 0;
+    size_t pack_total_ = 0;
     // tensor-core weight gradients: one plan per convolution, per-group partial sums
     std::vector<dn::TcWgradPlan> plans_wg_;
     float *partial_wg_ = nullptr;
+    float *bias_part_ = nullptr;  // per-block bias-gradient sums (dn::grad_prep)
     float *out_ = nullptr, *gout_ = nullptr, *gtmp_ = nullptr;
     const __half *feat_ = nullptr;  // features of the last forward (the caller's buffer; used until the call returns)
     int *err_ = nullptr;

@@ -188,6 +188,40 @@ __global__ void k_grad_bf16(const float *g, __nv_bfloat16 *out, size_t pixels, i
     }
 }
 
+// Threads (r, k), r < rows, k < c_pad: channel k of pixels p0 + r, p0 + r +
+// rows, ... of the block's range; reads and writes are row-contiguous.
+__global__ void k_grad_prep(const __nv_bfloat16 *y, const float *g, __nv_bfloat16 *out, float *part, size_t pixels,
+                            size_t chunk, int c, int c_pad, int rows) {
+    __shared__ float sm[256];
+    const int k = (int)threadIdx.x % c_pad, r = (int)threadIdx.x / c_pad;
+    const size_t p0 = (size_t)blockIdx.x * chunk, p1 = p0 + chunk < pixels ? p0 + chunk : pixels;
+    float acc = 0.f;
+    for (size_t p = p0 + r; p < p1; p += rows) {
+        float v = 0.f;
+        if (k < c) {
+            v = g[p * c + k];
+            if (y && !(bf(y[p * c + k]) > 0.f)) v = 0.f;
+        }
+        out[p * c_pad + k] = __float2bfloat16(v);
+        acc += v;
+    }
+    sm[threadIdx.x] = acc;
+    __syncthreads();
+    if (r == 0 && k < c) {
+        float s = 0.f;
+        for (int i = 0; i < rows; i++) s += sm[i * c_pad + k];
+        part[(size_t)blockIdx.x * c + k] = s;
+    }
+}
+
+__global__ void k_bias_finalize(const float *part, float *db, int blocks, int c) {
+    const int k = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (k >= c) return;
+    float s = 0.f;
+    for (int b = 0; b < blocks; b++) s += part[(size_t)b * c + k];
+    db[k] += s;
+}
+
 __global__ void k_bias_grad(const float *g, float *db, size_t pixels, int c) {
     // one block per channel
     __shared__ float sm[256];
@@ -382,6 +416,18 @@ cudaError_t relu_mask(const __nv_bfloat16 *y, const float *g, float *out, size_t
 }
 cudaError_t bias_grad(const float *g, float *db, size_t pixels, int c, cudaStream_t st) {
     k_bias_grad<<<c, 256, 0, st>>>(g, db, pixels, c);
+    return cudaGetLastError();
+}
+cudaError_t grad_prep(const __nv_bfloat16 *y, const float *g, __nv_bfloat16 *out, float *part, float *db,
+                      size_t pixels, int c, int c_pad, cudaStream_t st) {
+    if (c_pad < c || c_pad > 256 || (c_pad & 15) || pixels == 0) return cudaErrorInvalidValue;
+    const int rows = 256 / c_pad;
+    const size_t chunk = (pixels + kGradPrepBlocks - 1) / kGradPrepBlocks;
+    const int blocks = (int)((pixels + chunk - 1) / chunk);
+    k_grad_prep<<<blocks, rows * c_pad, 0, st>>>(y, g, out, part, pixels, chunk, c, c_pad, rows);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_bias_finalize<<<(c + 127) / 128, 128, 0, st>>>(part, db, blocks, c);
     return cudaGetLastError();
 }
 cudaError_t grad_bf16(const float *g, __nv_bfloat16 *out, size_t pixels, int c, int c_pad, cudaStream_t st) {

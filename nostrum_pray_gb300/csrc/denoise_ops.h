@@ -38,6 +38,19 @@ cudaError_t tc_pack_weights(const float *w, __nv_bfloat16 *packed, int cin, int 
 // cin = cout_f rounded up to 16 and cout = cin_f runs it on the output
 // gradient (as BF16, grad_bf16) and writes the input gradient.
 cudaError_t tc_pack_weights_bwd(const float *w, __nv_bfloat16 *packed, int cin_f, int cout_f, cudaStream_t st);
+// Every packing of a network's weights in one launch: job j packs w (the
+// FP32 [cout_f][9][cin_f] weights of one convolution) into out, as
+// tc_pack_weights (bwd 0: cin_pad = cin_f rounded up to 16, npad = cout_f
+// rounded up) or tc_pack_weights_bwd (bwd 1: cin_pad = cout_f rounded up,
+// npad = cin_f rounded up) does; its 9 x cin_pad x npad elements start at
+// `begin` of the concatenated range, jobs in increasing begin (at most 64).
+struct TcPackJob {
+    const float *w;
+    __nv_bfloat16 *out;
+    unsigned long long begin;
+    int cin_f, cout_f, cin_pad, npad, bwd;
+};
+cudaError_t tc_pack_all(const TcPackJob *jobs_dev, int njobs, size_t total, cudaStream_t st);
 cudaError_t conv3x3_forward_tc(const TcConvPlan &p, const __nv_bfloat16 *wpacked, const float *bias,
                                __nv_bfloat16 *y, float *y32, float *partial, int *err, cudaStream_t st);
 // Weight gradient of a 3x3 convolution on the tensor cores:
@@ -53,8 +66,8 @@ struct TcWgradPlan {
     alignas(64) unsigned char gmap[128];  // CUtensorMap of g: (cout_pad, W, H, N), box (8, 8, 16, 1)
     const __nv_bfloat16 *g;
     int n, h, w, cin, cin_pad, cout, cout_pad;
-    int tiles_x, tiles_y, tiles, tiles_per_cta, groups, taps_per_pass, passes, tmem_cols;
-    uint32_t b_off, bar_off;
+    int tiles_x, tiles_y, tiles, tiles_per_cta, groups, taps_per_pass, passes, tmem_cols, stages;
+    uint32_t b_off, stage_bytes, bar_off;
     size_t smem, partial_floats;
 };
 cudaError_t tc_wgrad_plan(TcWgradPlan &p, const __nv_bfloat16 *g, int n, int h, int w, int cin, int cin_pad, int cout,
@@ -69,6 +82,14 @@ cudaError_t conv3x3_backward(const __nv_bfloat16 *x, const __nv_bfloat16 *w, con
 cudaError_t relu_mask(const __nv_bfloat16 *y, const float *g, float *out, size_t n, cudaStream_t st);
 // db[c] += sum over pixels of g[p][c]
 cudaError_t bias_grad(const float *g, float *db, size_t pixels, int c, cudaStream_t st);
+// One pass over a convolution's output gradient g (pixels x c FP32) for the
+// tensor-core backward: the ReLU mask of the convolution's output y (NULL:
+// no mask), the masked gradient as BF16 with c_pad >= c channels (the pad
+// zero), and the bias gradient: per-block partial sums in part
+// (kGradPrepBlocks x c floats), added in block order into db.
+constexpr int kGradPrepBlocks = 1024;
+cudaError_t grad_prep(const __nv_bfloat16 *y, const float *g, __nv_bfloat16 *out, float *part, float *db,
+                      size_t pixels, int c, int c_pad, cudaStream_t st);
 // g (pixels x c FP32) as BF16 with c_pad >= c channels (the pad zero)
 cudaError_t grad_bf16(const float *g, __nv_bfloat16 *out, size_t pixels, int c, int c_pad, cudaStream_t st);
 cudaError_t avgpool(const __nv_bfloat16 *x, __nv_bfloat16 *y, int n, int h, int w, int c, cudaStream_t st);

@@ -485,19 +485,20 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_tc_persistent(const __grid_
 //      along K and one plane apart along N.
 // So every tap reads the same halo, shifted by whole 16-byte pixels, as in
 // the forward pass. Each CTA owns a group of tiles and a group of taps
-// (tensor memory holds taps_per_pass x cin_pad FP32 columns), loads a tile's
-// planes, issues its MMAs, and waits for them before loading the next tile.
-// The accumulators go to partial[group][tap][co][ci]; k_wgrad_finalize adds
-// the groups in order into dw. Every wait is bounded (error flag, drain,
-// TMEM freed).
+// (tensor memory holds taps_per_pass x cin_pad FP32 columns). One thread
+// loads the tiles into two shared-memory stages, the next tile's planes
+// while the tensor cores work on this one's (one stage where two do not
+// fit), and issues the MMAs. The accumulators of the output channels below
+// cout go to partial[group][tap][co][ci]; k_wgrad_finalize adds the groups in
+// order into dw. Every wait is bounded (error flag, drain, TMEM freed).
 constexpr uint32_t kGradPlaneBytes = kTileW * kTileH * 16;  // 2,048
 constexpr int kGradPlanes = 16;                             // 128 rows of A
 
 struct WgArgs {
-    float *partial;  // [group][9][128][cin_pad]
-    int n, h, wd, cin_pad, cout_pad;
-    int tiles_x, tiles_y, tiles, tiles_per_cta, taps_per_pass, tmem_cols;
-    uint32_t b_off, bar_off;
+    float *partial;  // [group][9][cout][cin_pad]
+    int n, h, wd, cin_pad, cout, cout_pad;
+    int tiles_x, tiles_y, tiles, tiles_per_cta, taps_per_pass, tmem_cols, stages;
+    uint32_t b_off, stage_bytes, bar_off;
     int *err;
 };
 
@@ -518,18 +519,24 @@ __global__ void __launch_bounds__(128) k_wgrad_tc(const __grid_constant__ CUtens
                                                   const __grid_constant__ CUtensorMap xmap, WgArgs P) {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int tid = threadIdx.x, warp = tid >> 5;
-    const uint32_t abase = smem_u32(smem), bbase = abase + P.b_off;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + P.bar_off);  // [0] tile loaded, [1] MMAs done
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2);
+    const int S = P.stages;
+    const uint32_t base = smem_u32(smem);
+    // bars[s] stage s loaded, bars[2 + s] MMAs reading stage s done, bars[4] drain
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + P.bar_off);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 5);
     int *okflag = reinterpret_cast<int *>(tmem_slot + 1);
     const int gplanes = P.cout_pad >> 3, xplanes = P.cin_pad >> 3;
     const int group = blockIdx.x, pass = blockIdx.y;
     const int tap0 = pass * P.taps_per_pass, ntaps = min(9 - tap0, P.taps_per_pass);
     const int t_begin = group * P.tiles_per_cta, t_end = min(P.tiles, t_begin + P.tiles_per_cta);
+    auto abase = [&](int st) { return base + (uint32_t)st * P.stage_bytes; };
+    auto bar = [&](int i) { return smem_u32(&bars[i]); };
 
-    // the rows of A above cout_pad stay zero
-    for (uint32_t i = (uint32_t)gplanes * kGradPlaneBytes / 16 + tid; i < kGradPlanes * kGradPlaneBytes / 16; i += 128)
-        reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0u, 0u, 0u, 0u);
+    // the rows of A above cout_pad stay zero, in every stage
+    for (int st = 0; st < S; st++)
+        for (uint32_t i = (uint32_t)gplanes * kGradPlaneBytes / 16 + tid; i < kGradPlanes * kGradPlaneBytes / 16;
+             i += 128)
+            reinterpret_cast<uint4 *>(smem + (size_t)st * P.stage_bytes)[i] = make_uint4(0u, 0u, 0u, 0u);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                      "r"(P.tmem_cols)
@@ -537,8 +544,7 @@ __global__ void __launch_bounds__(128) k_wgrad_tc(const __grid_constant__ CUtens
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        mbar_init(smem_u32(&bars[0]));
-        mbar_init(smem_u32(&bars[1]));
+        for (int i = 0; i < 5; i++) mbar_init(bar(i));
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the zero rows, for the tensor cores
@@ -552,55 +558,79 @@ __global__ void __launch_bounds__(128) k_wgrad_tc(const __grid_constant__ CUtens
         const uint32_t idesc = inst_desc_mn(128, P.cin_pad);
         const uint32_t bytes = (uint32_t)gplanes * kGradPlaneBytes + (uint32_t)xplanes * kChunkBytes;
         const int per_img = P.tiles_x * P.tiles_y;
-        uint32_t phase = 0;
-        bool first = true;
-        for (int t = t_begin; t < t_end && ok; t++, phase ^= 1u) {
+        const int n = t_end > t_begin ? t_end - t_begin : 0;
+        // tile i of the group goes to stage i % S; issue() starts its loads
+        auto issue = [&](int i) {
+            const int t = t_begin + i, st = i % S;
             const int img = t / per_img, rem = t - img * per_img;
             const int y0 = (rem / P.tiles_x) * kTileH, x0 = (rem % P.tiles_x) * kTileW;
-            // the previous tile's MMAs read these buffers: they completed (bars[1]) before this load
-            mbar_expect_tx(smem_u32(&bars[0]), bytes);
-            for (int c = 0; c < gplanes; c++)
-                tma_tile(abase + c * kGradPlaneBytes, &gmap, smem_u32(&bars[0]), 8 * c, x0, y0, img);
+            const uint32_t a = abase(st), b = a + P.b_off;
+            mbar_expect_tx(bar(st), bytes);
+            for (int c = 0; c < gplanes; c++) tma_tile(a + c * kGradPlaneBytes, &gmap, bar(st), 8 * c, x0, y0, img);
             for (int c = 0; c < xplanes; c++)
-                tma_halo(bbase + c * kPlaneBytes, &xmap, smem_u32(&bars[0]), 8 * c, x0 - 1, y0 - 1, img);
-            if (!mbar_wait(smem_u32(&bars[0]), phase)) {
+                tma_halo(b + c * kPlaneBytes, &xmap, bar(st), 8 * c, x0 - 1, y0 - 1, img);
+        };
+        int issued = 0, consumed = 0, committed = 0;
+        if (n > 0) issue(issued++);
+        for (int i = 0; i < n && ok; i++) {
+            const int st = i % S;
+            // with two stages, load tile i + 1 into the other stage as soon as
+            // the MMAs of tile i - 1, which read it, are done
+            if (S == 2 && i + 1 < n) {
+                if (i >= 1 && !mbar_wait(bar(2 + (st ^ 1)), (uint32_t)((i - 1) / 2) & 1u)) {
+                    ok = false;
+                    break;
+                }
+                issue(issued++);
+            }
+            if (!mbar_wait(bar(st), (uint32_t)(i / S) & 1u)) {
                 ok = false;
                 break;
             }
+            consumed = i + 1;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t a = abase(st), b = a + P.b_off;
             for (int q = 0; q < ntaps; q++) {
                 const int tap = tap0 + q, dy = tap / 3, dx = tap - 3 * (tap / 3);
                 const uint32_t d = tmem + (uint32_t)(q * P.cin_pad);
                 for (int k = 0; k < kTileH / 2; k++) {
-                    const uint64_t ad = smem_desc(abase + (uint32_t)k * 256u, 128u, kGradPlaneBytes);
+                    const uint64_t ad = smem_desc(a + (uint32_t)k * 256u, 128u, kGradPlaneBytes);
                     const uint64_t bd =
-                        smem_desc(bbase + (uint32_t)((2 * k + dy) * kHaloW + dx) * 16u, kRowBytes, kPlaneBytes);
-                    mma(d, ad, bd, idesc, (first && k == 0) ? 0u : 1u);
+                        smem_desc(b + (uint32_t)((2 * k + dy) * kHaloW + dx) * 16u, kRowBytes, kPlaneBytes);
+                    mma(d, ad, bd, idesc, (i == 0 && k == 0) ? 0u : 1u);
                 }
             }
-            first = false;
-            commit(smem_u32(&bars[1]));
-            if (!mbar_wait(smem_u32(&bars[1]), phase)) {
-                ok = false;
-                break;
+            commit(bar(2 + st));
+            committed = i + 1;
+            if (S == 1) {
+                // one stage: the next load waits for this tile's MMAs
+                if (!mbar_wait(bar(2), (uint32_t)i & 1u)) {
+                    ok = false;
+                    break;
+                }
+                if (i + 1 < n) issue(issued++);
             }
         }
-        *okflag = !ok ? 0 : (first ? 2 : 1);  // 2: no tile in this group
+        if (ok && n > 0 && S == 2 && !mbar_wait(bar(2 + (n - 1) % 2), (uint32_t)((n - 1) / 2) & 1u)) ok = false;
+        *okflag = !ok ? 0 : (n == 0 ? 2 : 1);  // 2: no tile in this group
         if (!ok) {
-            // bounded drain of what may still be in flight
-            mbar_wait(smem_u32(&bars[0]), phase);
-            commit(smem_u32(&bars[1]));
-            mbar_wait(smem_u32(&bars[1]), phase);
+            // bounded drain: copies still in flight, then every MMA issued
+            for (int j = consumed; j < issued; j++) mbar_wait(bar(j % S), (uint32_t)(j / S) & 1u);
+            if (committed > 0) {
+                commit(bar(4));
+                mbar_wait(bar(4), 0);
+            }
         }
     }
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const int flag = *okflag;
     if (flag == 0 && tid == 0) atomicExch(P.err, 1);
-    // epilogue: warp q reads TMEM lanes 32q..32q+31 (rows co), all columns
+    // epilogue: warp q reads TMEM lanes 32q..32q+31 (rows co), all columns;
+    // rows from cout on are zero padding and are not stored
     const int co = warp * 32 + (tid & 31);
-    for (int q = 0; q < ntaps; q++) {
-        float *dst = P.partial + (((size_t)group * 9 + tap0 + q) * 128 + co) * P.cin_pad;
+    for (int q = 0; q < ntaps && warp * 32 < P.cout; q++) {
+        float *dst = P.partial + (((size_t)group * 9 + tap0 + q) * P.cout + co) * P.cin_pad;
         for (int c0 = 0; c0 < P.cin_pad; c0 += 16) {
             uint32_t r[16];
             const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(q * P.cin_pad + c0);
@@ -613,6 +643,7 @@ __global__ void __launch_bounds__(128) k_wgrad_tc(const __grid_constant__ CUtens
                 : "r"(taddr)
                 : "memory");
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (co >= P.cout) continue;
             float4 *o = reinterpret_cast<float4 *>(dst + c0);
 #pragma unroll
             for (int k = 0; k < 4; k++) {
@@ -641,7 +672,7 @@ __global__ void k_wgrad_finalize(const float *partial, float *dw, int groups, in
         const size_t rest = i / cin;
         const int tap = (int)(rest % 9), co = (int)(rest / 9);
         float v = 0.f;
-        for (int g = 0; g < groups; g++) v += partial[(((size_t)g * 9 + tap) * 128 + co) * cin_pad + ci];
+        for (int g = 0; g < groups; g++) v += partial[(((size_t)g * 9 + tap) * cout + co) * cin_pad + ci];
         dw[i] += v;
     }
 }
@@ -721,6 +752,31 @@ __global__ void k_pack_weights_bwd(const float *w, __nv_bfloat16 *out, int cin_f
     }
 }
 
+__global__ void k_pack_all(const TcPackJob *jobs, int njobs, size_t total) {
+    __shared__ TcPackJob sj[64];
+    for (int i = (int)threadIdx.x; i < njobs; i += (int)blockDim.x) sj[i] = jobs[i];
+    __syncthreads();
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        int j = 0;
+        while (j + 1 < njobs && sj[j + 1].begin <= i) j++;
+        const TcPackJob &J = sj[j];
+        const size_t li = i - J.begin;
+        const int e = (int)(li & 7);
+        const size_t rowi = li >> 3;
+        const int r = (int)(rowi % J.npad);
+        const size_t ct = rowi / J.npad;
+        const int nchunk = J.cin_pad >> 3;
+        const int chunk = (int)(ct % nchunk), tap = (int)(ct / nchunk);
+        const int c = chunk * 8 + e;
+        float v;
+        if (!J.bwd)  // row r = output channel, c = input channel
+            v = (r < J.cout_f && c < J.cin_f) ? J.w[((size_t)r * 9 + tap) * J.cin_f + c] : 0.f;
+        else  // transposed, taps mirrored: row r = input channel, c = output channel
+            v = (r < J.cin_f && c < J.cout_f) ? J.w[((size_t)c * 9 + (8 - tap)) * J.cin_f + r] : 0.f;
+        J.out[li] = __float2bfloat16(v);
+    }
+}
+
 unsigned grid_for(size_t n) {
     const size_t b = (n + 255) / 256;
     return (unsigned)(b < 4096 ? (b ? b : 1) : 4096);
@@ -751,6 +807,12 @@ cudaError_t tc_pack_weights(const float *w, __nv_bfloat16 *packed, int cin, int 
     const int npad = (cout + 15) / 16 * 16;
     k_pack_weights<<<grid_for(tc_packed_weight_elems(cin_pad, cout)), 256, 0, st>>>(w, packed, cin, cin_pad, cout,
                                                                                    npad);
+    return cudaGetLastError();
+}
+
+cudaError_t tc_pack_all(const TcPackJob *jobs_dev, int njobs, size_t total, cudaStream_t st) {
+    if (njobs <= 0 || njobs > 64) return cudaErrorInvalidValue;
+    k_pack_all<<<grid_for(total), 256, 0, st>>>(jobs_dev, njobs, total);
     return cudaGetLastError();
 }
 
@@ -786,9 +848,13 @@ cudaError_t tc_wgrad_plan(TcWgradPlan &p, const __nv_bfloat16 *g, int n, int h, 
     if (per < 1) per = 1;
     p.tiles_per_cta = (int)per;
     p.groups = (int)((tiles + per - 1) / per);
+    // a stage: 128 rows of A (16 planes), then the halo planes of B; two
+    // stages (loads of the next tile beside the MMAs of this one) where they fit
     p.b_off = kGradPlanes * kGradPlaneBytes;
-    p.bar_off = (p.b_off + (uint32_t)(cin_pad / 8) * kPlaneBytes + 15) & ~15u;
-    p.smem = p.bar_off + 2 * 8 + 16;
+    p.stage_bytes = (p.b_off + (uint32_t)(cin_pad / 8) * kPlaneBytes + 1023) & ~1023u;
+    p.stages = 2 * (size_t)p.stage_bytes + 64 <= kSmemMax ? 2 : 1;
+    p.bar_off = (uint32_t)p.stages * p.stage_bytes;
+    p.smem = p.bar_off + 5 * 8 + 16;
     if (p.smem > kSmemMax) return cudaErrorInvalidValue;
     // no more CTAs per SM than TMEM has columns for (tcgen05.alloc would wait):
     // ask for enough shared memory to keep the others off the SM
@@ -797,7 +863,7 @@ cudaError_t tc_wgrad_plan(TcWgradPlan &p, const __nv_bfloat16 *g, int n, int h, 
         p.smem = kSmemPerSm / max_ctas - 1024 + 16;
         if (p.smem > kSmemMax) p.smem = kSmemMax;
     }
-    p.partial_floats = (size_t)p.groups * 9 * 128 * cin_pad;
+    p.partial_floats = (size_t)p.groups * 9 * cout * cin_pad;
     EncodeTiled enc = encode_fn();
     if (!enc) return cudaErrorNotSupported;
     const cuuint64_t dims[4] = {(cuuint64_t)p.cout_pad, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
@@ -828,10 +894,10 @@ cudaError_t conv3x3_wgrad_tc(const TcWgradPlan &p, const TcConvPlan &fwd, float 
     }
     WgArgs a;
     a.partial = partial;
-    a.n = p.n, a.h = p.h, a.wd = p.w, a.cin_pad = p.cin_pad, a.cout_pad = p.cout_pad;
+    a.n = p.n, a.h = p.h, a.wd = p.w, a.cin_pad = p.cin_pad, a.cout = p.cout, a.cout_pad = p.cout_pad;
     a.tiles_x = p.tiles_x, a.tiles_y = p.tiles_y, a.tiles = p.tiles, a.tiles_per_cta = p.tiles_per_cta;
-    a.taps_per_pass = p.taps_per_pass, a.tmem_cols = p.tmem_cols;
-    a.b_off = p.b_off, a.bar_off = p.bar_off;
+    a.taps_per_pass = p.taps_per_pass, a.tmem_cols = p.tmem_cols, a.stages = p.stages;
+    a.b_off = p.b_off, a.stage_bytes = p.stage_bytes, a.bar_off = p.bar_off;
     a.err = err;
     CUtensorMap gm, xm;
     std::memcpy(&gm, p.gmap, sizeof(gm));
