@@ -214,12 +214,21 @@ __global__ void k_grad_prep(const __nv_bfloat16 *y, const float *g, __nv_bfloat1
     }
 }
 
+// One block (256 threads) per channel: thread t adds the partials of blocks
+// t, t + 256, ..., then a fixed tree adds the 256 sums (the same order on
+// every run).
 __global__ void k_bias_finalize(const float *part, float *db, int blocks, int c) {
-    const int k = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    if (k >= c) return;
+    __shared__ float sm[256];
+    const int k = (int)blockIdx.x, t = (int)threadIdx.x;
     float s = 0.f;
-    for (int b = 0; b < blocks; b++) s += part[(size_t)b * c + k];
-    db[k] += s;
+    for (int b = t; b < blocks; b += 256) s += part[(size_t)b * c + k];
+    sm[t] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (t < o) sm[t] += sm[t + o];
+        __syncthreads();
+    }
+    if (t == 0) db[k] += sm[0];
 }
 
 __global__ void k_bias_grad(const float *g, float *db, size_t pixels, int c) {
@@ -427,7 +436,7 @@ cudaError_t grad_prep(const __nv_bfloat16 *y, const float *g, __nv_bfloat16 *out
     k_grad_prep<<<blocks, rows * c_pad, 0, st>>>(y, g, out, part, pixels, chunk, c, c_pad, rows);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_bias_finalize<<<(c + 127) / 128, 128, 0, st>>>(part, db, blocks, c);
+    k_bias_finalize<<<c, 256, 0, st>>>(part, db, blocks, c);
     return cudaGetLastError();
 }
 cudaError_t grad_bf16(const float *g, __nv_bfloat16 *out, size_t pixels, int c, int c_pad, cudaStream_t st) {

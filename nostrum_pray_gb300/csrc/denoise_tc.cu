@@ -665,15 +665,29 @@ __global__ void __launch_bounds__(128) k_wgrad_tc(const __grid_constant__ CUtens
 }
 
 // dw[co][tap][ci] += sum over groups (in order) of partial[group][tap][co][ci]
+// Block of 256 threads: 32 consecutive gradient elements x 8 slices; slice
+// s adds groups s, s + 8, ..., and the 8 slice sums are added in slice order
+// (the same order on every run).
+constexpr int kFinSlices = 8;
 __global__ void k_wgrad_finalize(const float *partial, float *dw, int groups, int cout, int cin, int cin_pad) {
+    __shared__ float sm[kFinSlices][32];
     const size_t total = (size_t)cout * 9 * cin;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int lane = (int)threadIdx.x & 31, slice = (int)threadIdx.x >> 5;
+    const size_t i = (size_t)blockIdx.x * 32 + lane;
+    float v = 0.f;
+    if (i < total) {
         const int ci = (int)(i % cin);
         const size_t rest = i / cin;
         const int tap = (int)(rest % 9), co = (int)(rest / 9);
-        float v = 0.f;
-        for (int g = 0; g < groups; g++) v += partial[(((size_t)g * 9 + tap) * cout + co) * cin_pad + ci];
-        dw[i] += v;
+        for (int g = slice; g < groups; g += kFinSlices)
+            v += partial[(((size_t)g * 9 + tap) * cout + co) * cin_pad + ci];
+    }
+    sm[slice][lane] = v;
+    __syncthreads();
+    if (slice == 0 && i < total) {
+        float s = sm[0][lane];
+        for (int k = 1; k < kFinSlices; k++) s += sm[k][lane];
+        dw[i] += s;
     }
 }
 
@@ -842,8 +856,9 @@ cudaError_t tc_wgrad_plan(TcWgradPlan &p, const __nv_bfloat16 *g, int n, int h, 
     int cols = 32;
     while (cols < p.taps_per_pass * cin_pad) cols <<= 1;
     p.tmem_cols = cols;
-    // about two CTAs per SM over all groups and passes
-    const long long want = 2LL * sm_count;
+    // about one CTA per SM over all groups and passes (a CTA overlaps its
+    // loads with its MMAs; fewer groups also mean fewer partial sums)
+    const long long want = sm_count;
     long long per = (tiles * p.passes + want - 1) / want;
     if (per < 1) per = 1;
     p.tiles_per_cta = (int)per;
@@ -904,8 +919,9 @@ cudaError_t conv3x3_wgrad_tc(const TcWgradPlan &p, const TcConvPlan &fwd, float 
     std::memcpy(&xm, fwd.tmap, sizeof(xm));
     k_wgrad_tc<<<dim3((unsigned)p.groups, (unsigned)p.passes), 128, p.smem, st>>>(gm, xm, a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    k_wgrad_finalize<<<grid_for((size_t)p.cout * 9 * p.cin), 256, 0, st>>>(partial, dw, p.groups, p.cout, p.cin,
-                                                                          p.cin_pad);
+    const size_t elems = (size_t)p.cout * 9 * p.cin;
+    k_wgrad_finalize<<<(unsigned)((elems + 31) / 32), 32 * kFinSlices, 0, st>>>(partial, dw, p.groups, p.cout, p.cin,
+                                                                             p.cin_pad);
     return cudaGetLastError();
 }
 
