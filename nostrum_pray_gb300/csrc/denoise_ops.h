@@ -25,6 +25,7 @@ struct TcConvPlan {
     const __nv_bfloat16 *x;
     int n, h, w, cin, cout, npad, relu;
     int tiles_x, tiles_y, tiles, splits, taps_per_split, taps_per_stage, stages, tmem_cols;
+    int nsplit, npad_full;  // output-channel split: nsplit CTAs per tile, npad channels each of npad_full
     int persistent, grid;  // persistent pipelined kernel (no split, weights resident) and its CTAs
     uint32_t w_off, bar_off, halo_stride;
     size_t smem, partial_floats;

@@ -62,6 +62,9 @@ struct TcArgs {
     int n, h, wd, cin, cout, npad, relu;
     int tiles_x, tiles_y;
     int taps_per_split, taps_per_stage, stages;
+    int nsplit;               // > 1: blockIdx.y picks output channels [y * npad, (y + 1) * npad), all taps,
+                              // the weight slice by TMA (wmap) from the packing of npad_full rows
+    int npad_full;
     int tmem_cols;
     uint32_t w_off, bar_off;  // shared-memory offsets (the halo is at 0)
     uint32_t halo_stride;     // persistent kernel: distance between the halo ring's slots
@@ -115,6 +118,16 @@ __device__ __forceinline__ void tma_halo(uint32_t dst, const CUtensorMap *map, u
         : "memory");
 }
 
+// A slice of packed weights: box (8 channels, npad rows, taps x chunks) of the
+// 3-D map (8, npad_full, 9 x cin / 8) at rows from n, (tap, chunk) from k.
+__device__ __forceinline__ void tma_w(uint32_t dst, const CUtensorMap *map, uint32_t bar, int n, int k) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], "
+        "[%2];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(0), "r"(n), "r"(k)
+        : "memory");
+}
+
 __device__ __forceinline__ void bulk_copy(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
                  "l"(src), "r"(bytes), "r"(bar)
@@ -143,7 +156,7 @@ __device__ __forceinline__ uint32_t pack2(float a, float b) {
 // (m / 8, m % 8)) from column `tmem` on, 16 columns at a time, and stores
 // bias + ReLU + BF16 (16-byte stores), FP32, or raw FP32 partials.
 __device__ __forceinline__ void epilogue(const TcArgs &P, uint32_t tmem, int img, int y0, int x0, int split,
-                                         int quad) {
+                                         int quad, int n0 = 0) {
     const int m = quad * 32 + (int)(threadIdx.x & 31);
     const int yy = y0 + (m >> 3), xx = x0 + (m & 7);
     const bool valid = yy < P.h && xx < P.wd;
@@ -172,26 +185,28 @@ __device__ __forceinline__ void epilogue(const TcArgs &P, uint32_t tmem, int img
             float v[16];
 #pragma unroll
             for (int k = 0; k < 16; k++) {
-                v[k] = __uint_as_float(r[k]) + __ldg(P.bias + c0 + k);
+                v[k] = __uint_as_float(r[k]) + __ldg(P.bias + n0 + c0 + k);
                 if (P.relu) v[k] = fmaxf(v[k], 0.f);
             }
-            uint4 *o = reinterpret_cast<uint4 *>(P.y + pix * P.cout + c0);
+            uint4 *o = reinterpret_cast<uint4 *>(P.y + pix * P.cout + n0 + c0);
             o[0] = make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
             o[1] = make_uint4(pack2(v[8], v[9]), pack2(v[10], v[11]), pack2(v[12], v[13]), pack2(v[14], v[15]));
         } else {
 #pragma unroll
             for (int k = 0; k < 16; k++) {
-                if (c0 + k >= P.cout) break;
-                float v = __uint_as_float(r[k]) + __ldg(P.bias + c0 + k);
+                const int co = n0 + c0 + k;
+                if (co >= P.cout) break;
+                float v = __uint_as_float(r[k]) + __ldg(P.bias + co);
                 if (P.relu) v = fmaxf(v, 0.f);
-                if (P.y) P.y[pix * P.cout + c0 + k] = __float2bfloat16(v);
-                if (P.y32) P.y32[pix * P.cout + c0 + k] = v;
+                if (P.y) P.y[pix * P.cout + co] = __float2bfloat16(v);
+                if (P.y32) P.y32[pix * P.cout + co] = v;
             }
         }
     }
 }
 
-__global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtensorMap xmap, TcArgs P) {
+__global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtensorMap xmap,
+                                                 const __grid_constant__ CUtensorMap wmap, TcArgs P) {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int tid = threadIdx.x, warp = tid >> 5;
     const int nchunk = P.cin >> 3;
@@ -206,9 +221,13 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtenso
     const int per_img = P.tiles_x * P.tiles_y;
     const int img = blockIdx.x / per_img, rem = blockIdx.x - img * per_img;
     const int y0 = (rem / P.tiles_x) * kTileH, x0 = (rem % P.tiles_x) * kTileW;
-    const int split = blockIdx.y;
+    // tap split (nsplit 1): blockIdx.y picks a group of taps; output-channel
+    // split: all taps, channels from n0
+    const int split = P.nsplit > 1 ? 0 : blockIdx.y;
+    const int n0 = P.nsplit > 1 ? (int)blockIdx.y * P.npad : 0;
     const int t0 = split * P.taps_per_split;
     const int nloads = P.taps_per_split / P.taps_per_stage;
+    const int kchunks = P.cin >> 3;  // 8-channel chunks per tap (the weight map's third coordinate)
     const uint32_t wtap_bytes = (uint32_t)P.cin * P.npad * 2;
     const uint32_t stage_bytes = wtap_bytes * P.taps_per_stage;
 
@@ -232,14 +251,20 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtenso
         // halo: one copy per 8-channel chunk, all completing on bars[0]
         mbar_expect_tx(bar(0), (uint32_t)nchunk * kChunkBytes);
         for (int c = 0; c < nchunk; c++) tma_halo(halo + c * kPlaneBytes, &xmap, bar(0), 8 * c, x0 - 1, y0 - 1, img);
-        // weights: the first `stages` loads
+        // weights: the first `stages` loads; with the output-channel split, one
+        // TMA box per load: rows n0..n0+npad of every (tap, chunk) of the stage
         int issued = 0;
         const __nv_bfloat16 *wsrc = P.w + (size_t)t0 * P.cin * P.npad;
-        for (; issued < nloads && issued < P.stages; issued++) {
-            mbar_expect_tx(bar(2 + issued), stage_bytes);
-            bulk_copy(wbase + issued * stage_bytes, wsrc + (size_t)issued * P.taps_per_stage * P.cin * P.npad,
-                      stage_bytes, bar(2 + issued));
-        }
+        auto load_weights = [&](int stage, int load) {
+            mbar_expect_tx(bar(2 + stage), stage_bytes);
+            if (P.nsplit > 1)
+                tma_w(wbase + stage * stage_bytes, &wmap, bar(2 + stage), n0,
+                      (t0 + load * P.taps_per_stage) * kchunks);
+            else
+                bulk_copy(wbase + stage * stage_bytes, wsrc + (size_t)load * P.taps_per_stage * P.cin * P.npad,
+                          stage_bytes, bar(2 + stage));
+        };
+        for (; issued < nloads && issued < P.stages; issued++) load_weights(issued, issued);
         const bool halo_done = mbar_wait(bar(0), 0);
         ok = halo_done;
         const uint32_t idesc = inst_desc(128, P.npad);
@@ -272,9 +297,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtenso
                     ok = false;
                     break;
                 }
-                mbar_expect_tx(bar(2 + sp), stage_bytes);
-                bulk_copy(wbase + sp * stage_bytes, wsrc + (size_t)issued * P.taps_per_stage * P.cin * P.npad,
-                          stage_bytes, bar(2 + sp));
+                load_weights(sp, issued);
                 issued++;
             }
         }
@@ -292,7 +315,7 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtenso
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     __syncthreads();
     if (!ok && tid == 0) atomicExch(P.err, 1);
-    if (ok) epilogue(P, tmem, img, y0, x0, split, warp);
+    if (ok) epilogue(P, tmem, img, y0, x0, split, warp, n0);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) {
@@ -937,13 +960,35 @@ cudaError_t tc_conv_plan(TcConvPlan &p, const __nv_bfloat16 *x, int n, int h, in
     const long long tiles = (long long)n * p.tiles_x * p.tiles_y;
     if (tiles > 0x7FFFFFFFLL) return cudaErrorInvalidValue;
     p.tiles = (int)tiles;
-    // split the taps when there are too few tiles to fill the GPU twice
+    // too few tiles to fill the GPU twice: split the output channels into
+    // chunks of a multiple of 16 (each CTA all nine taps for its chunk, so no
+    // partial sums), the widest chunk that still gives one CTA per SM (every
+    // chunk's CTA loads the whole input halo, so narrower chunks cost loads);
+    // with a single 16-channel chunk, split the taps instead (partial sums and
+    // a finalize pass)
     p.splits = 1;
-    if (tiles < 2LL * sm_count) p.splits = (tiles * 3 >= 2LL * sm_count) ? 3 : 9;
+    p.nsplit = 1;
+    p.npad_full = p.npad;
+    if (tiles < 2LL * sm_count) {
+        if (p.npad >= 32) {
+            int cw = 16;
+            for (int c = p.npad / 2 / 16 * 16; c >= 16; c -= 16)
+                if (p.npad % c == 0 && tiles * (p.npad / c) >= (long long)sm_count) {
+                    cw = c;
+                    break;
+                }
+            p.nsplit = p.npad / cw;
+            p.npad = cw;
+        } else {
+            p.splits = (tiles * 3 >= 2LL * sm_count) ? 3 : 9;
+        }
+    }
     p.taps_per_split = 9 / p.splits;
     const size_t halo = (size_t)(cin / 8) * kPlaneBytes;
     const size_t wtap = (size_t)cin * p.npad * 2;
-    if (halo + p.taps_per_split * wtap <= kSmemBudget) {
+    // a TMA box of the weight slice spans at most 256 (tap, chunk) rows
+    const bool box_ok = p.nsplit == 1 || (size_t)p.taps_per_split * (cin / 8) <= 256;
+    if (halo + p.taps_per_split * wtap <= kSmemBudget && box_ok) {
         p.taps_per_stage = p.taps_per_split;
         p.stages = 1;
     } else {
@@ -952,8 +997,9 @@ cudaError_t tc_conv_plan(TcConvPlan &p, const __nv_bfloat16 *x, int n, int h, in
         if (fit < 2) fit = 2;
         p.stages = (int)(fit < (size_t)p.taps_per_split ? fit : (size_t)p.taps_per_split);
     }
+    if (p.nsplit > 1 && (size_t)p.taps_per_stage * (cin / 8) > 256) return cudaErrorInvalidValue;
     // persistent pipelined kernel: no split, two halos and all weights resident
-    p.persistent = p.splits == 1 && 2 * halo + 9 * wtap + 64 <= kSmemPersistent;
+    p.persistent = p.splits == 1 && p.nsplit == 1 && 2 * halo + 9 * wtap + 64 <= kSmemPersistent;
     size_t smem;
     int cols = 32;
     if (p.persistent) {
@@ -1038,15 +1084,32 @@ cudaError_t conv3x3_forward_tc(const TcConvPlan &p, const __nv_bfloat16 *wpacked
     a.n = p.n, a.h = p.h, a.wd = p.w, a.cin = p.cin, a.cout = p.cout, a.npad = p.npad, a.relu = p.relu;
     a.tiles_x = p.tiles_x, a.tiles_y = p.tiles_y;
     a.taps_per_split = p.taps_per_split, a.taps_per_stage = p.taps_per_stage, a.stages = p.stages;
+    a.nsplit = p.nsplit, a.npad_full = p.npad_full;
     a.tmem_cols = p.tmem_cols;
     a.w_off = p.w_off, a.bar_off = p.bar_off, a.halo_stride = p.halo_stride;
     a.err = err;
-    CUtensorMap map;
+    CUtensorMap map, wmap;
     std::memcpy(&map, p.tmap, sizeof(map));
+    std::memset(&wmap, 0, sizeof(wmap));
+    if (p.nsplit > 1) {
+        // the packed weights [tap][chunk][npad_full rows][8] as a 3-D map:
+        // (8 channels, rows, tap x chunk); each CTA loads rows n0..n0+npad
+        EncodeTiled enc = encode_fn();
+        if (!enc) return cudaErrorNotSupported;
+        const cuuint64_t dims[3] = {8, (cuuint64_t)p.npad_full, (cuuint64_t)9 * (p.cin / 8)};
+        const cuuint64_t strides[2] = {16, (cuuint64_t)p.npad_full * 16};
+        const cuuint32_t box[3] = {8, (cuuint32_t)p.npad, (cuuint32_t)(p.taps_per_stage * (p.cin / 8))};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        const CUresult r = enc(&wmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16 *>(wpacked), dims,
+                               strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+    }
     if (p.persistent)
         k_conv_tc_persistent<<<(unsigned)p.grid, kWsThreads, p.smem, st>>>(map, a);
     else
-        k_conv_tc<<<dim3((unsigned)p.tiles, (unsigned)p.splits), 128, p.smem, st>>>(map, a);
+        k_conv_tc<<<dim3((unsigned)p.tiles, (unsigned)(p.nsplit > 1 ? p.nsplit : p.splits)), 128, p.smem, st>>>(
+            map, wmap, a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || p.splits == 1) return e;
     const size_t M = (size_t)p.n * p.h * p.w;

@@ -71,12 +71,14 @@ def denoise_launches(h: int, w: int, n: int = 1, sm_count: int = 152, tensor_cor
     """Kernels one pray_denoise call launches: input packing, 4 poolings, 4
     upsample-concatenations, the 19 convolutions, the residual add and the
     output transform. On the tensor cores a convolution with fewer than two
-    16x8-pixel tiles per SM splits its taps and adds a finalize kernel (the
+    16x8-pixel tiles per SM splits its output channels over CTAs, or, with
+    a single 16-channel chunk, its taps, which adds a finalize kernel (the
     rule of tc_conv_plan in csrc/denoise_tc.cu)."""
     convs = 0
-    for _, _, l in CONVS:
+    for _, co, l in CONVS:
         tiles = n * -(-(w >> l) // 8) * -(-(h >> l) // 16)
-        convs += 2 if tensor_cores and tiles < 2 * sm_count else 1
+        npad = -(-co // 16) * 16
+        convs += 2 if tensor_cores and tiles < 2 * sm_count and npad < 32 else 1
     return 1 + 4 + 4 + convs + 2
 
 
