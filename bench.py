@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--dn-spp-in", type=int, default=4, help="denoise: samples per pixel of the noisy input")
     ap.add_argument("--dn-depth-in", type=int, default=0,
                     help="denoise: path depth of the noisy input (0: the full depth of the references)")
+    ap.add_argument("--dn-rr-in", type=int, default=-1,
+                    help="denoise: Russian roulette from this depth in the noisy input (-1: from depth 3, as the "
+                         "references and plain renders)")
     ap.add_argument("--dn-ref-spp", type=int, default=1024, help="denoise: training target samples per pixel")
     ap.add_argument("--dn-eval-ref-spp", type=int, default=4096,
                     help="denoise: samples per pixel of the held-out rooms' references")
@@ -279,13 +282,15 @@ def run_ours(args):
     kernel_ms_max = replicas.slowest(kernel_ms, "cuda")
     value = replicas.whole_job_rate(rays_per_frame * args.steps, kernel_ms / 1e3, "cuda") / 1e6
 
-    # end to end through the host-memory C ABI entry point (params in, image out)
+    # end to end through the host-memory C ABI entry point (params in, image
+    # out into a pinned host frame that the loop reuses)
+    h_img = torch.empty((setup.height, setup.width, 3), dtype=torch.uint8).pin_memory().numpy()
     for _ in range(2):
-        sc.render_rt_host(setup)
+        sc.render_rt_host(setup, out=h_img)
     e2e_times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        img, _ = sc.render_rt_host(setup)
+        img, _ = sc.render_rt_host(setup, out=h_img)
         e2e_times.append(time.perf_counter() - t0)
     e2e_val = replicas.whole_job_rate(rays_per_frame, statistics.mean(e2e_times), "cuda") / 1e6
 
@@ -511,9 +516,12 @@ def run_cornell(args):
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     rgb = torch.empty((st.height, st.width, 3), dtype=torch.uint8, device="cuda")
     ms = _timed_frames(lambda: sc.render_pt(p, rgb), args.steps, args.warmup, flush)
+    h_img = torch.empty((st.height, st.width, 3), dtype=torch.uint8).pin_memory().numpy()
+    h_rad = torch.empty((st.height, st.width, 3), dtype=torch.float32).pin_memory().numpy()
+    sc.render_pt_host(p, out=h_img, out_radiance=h_rad)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        sc.render_pt_host(p)
+        sc.render_pt_host(p, out=h_img, out_radiance=h_rad)
     e2e = time.perf_counter() - t0
     sec = ms / 1e3
     line = {"metric": "frames/s", "value": round(args.steps / sec, 3), "unit": "frames/s", "n_gpus": 1,
@@ -521,7 +529,7 @@ def run_cornell(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "reference example",
             "config": cfg, "mrays_per_s": round(segs * args.steps / sec / 1e6, 1), "segments_per_frame": segs,
             "e2e": {"value": round(args.steps / e2e, 3), "unit": "frames/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 3 * st.width * st.height}}
+                    "d2h_bytes_per_step": 15 * st.width * st.height}}
     sc.close()
     return line
 
@@ -558,7 +566,7 @@ def run_denoise(args):
     torch.cuda.set_device(0)
     cfg = D.DenoiseConfig(res=args.dn_res, train_res=args.dn_train_res, spp_ref=args.dn_ref_spp,
                           train_rooms=args.dn_train, eval_rooms=args.dn_eval, steps=args.dn_steps,
-                          spp_in=args.dn_spp_in, depth_in=args.dn_depth_in)
+                          spp_in=args.dn_spp_in, depth_in=args.dn_depth_in, rr_in=args.dn_rr_in)
     t0 = time.perf_counter()
     train_seeds = list(range(cfg.seed, cfg.seed + cfg.train_rooms))
     eval_seeds = list(range(cfg.seed + 100_000, cfg.seed + 100_000 + cfg.eval_rooms))
@@ -587,7 +595,8 @@ def run_denoise(args):
     line = {"metric": "time to relMSE<=0.01, denoised / plain", "value": round(float(np.mean(td) / np.mean(tp)), 4)
             if tp else None, "unit": "ratio", "n_gpus": 1, "higher_is_better": False, "dtype": "bf16",
             "data": "synthetic", "config": {"workload": f"procedural rooms, evaluated at {cfg.res}x{cfg.res}, {cfg.spp_in} spp input"
-                                                        f"{f' (paths cut at {cfg.depth_in} bounces)' if cfg.depth_in else ''},"
+                                                        f"{f' (paths cut at {cfg.depth_in} bounces)' if cfg.depth_in else ''}"
+                                                        f"{f' (Russian roulette from depth {cfg.rr_in})' if cfg.rr_in >= 0 else ''},"
                                                         f" path depth {cfg.depth} (RR from {cfg.rr_depth}),"
                                                         f" {cfg.spp_ref} spp FP64 training targets,"
                                                         f" {eval_cfg.spp_ref} spp FP64 evaluation references, {cfg.train_rooms} train rooms"
@@ -596,10 +605,17 @@ def run_denoise(args):
             "relmse_noisy_mean": float(np.mean([r["relmse_noisy"] for r in rows])),
             "relmse_denoised_mean": float(np.mean([r["relmse_denoised"] for r in rows])),
             "relmse_final_mean": float(np.mean([r["relmse_final"] for r in rows])),
+            "value_with_prediction": round(float(np.mean([r["time_final_with_prediction_s"] for r in rows])
+                                                 / np.mean(tp)), 4) if tp else None,
+            "prediction_note": "value: denoised time = input render + features + inference, plain time = one render at "
+                               "the smallest sample count that meets the target (known from the reference); neither "
+                               "side pays for estimating its error. value_with_prediction adds the fallback decision "
+                               "(a second input render and inference, and the relMSE between the two outputs read back)",
             "rooms_meeting_target": ok_d, "fallbacks": sum(r["fallback"] for r in rows), "fallback_spp": fb_spp,
             "time_plain_mean_s": float(np.mean(tp)) if tp else None, "time_denoised_mean_s": float(np.mean(td)),
             "render_input_mean_s": float(np.mean([r["render_s"] for r in rows])),
             "inference_mean_s": float(np.mean([r["inference_s"] for r in rows])),
+            "time_with_prediction_mean_s": float(np.mean([r["time_with_prediction_s"] for r in rows])),
             "spp_plain_to_target": [r["spp_plain_to_target"] for r in rows],
             "loss_first_last": [losses[0][1], losses[-1][1]], "data_s": round(data_s, 1),
             "train_s": round(train_s, 1), "eval_s": round(eval_s, 1),
@@ -618,7 +634,7 @@ def run_denoise_secondary(args):
     --dn-eval-ref-spp 4096`."""
     sub = argparse.Namespace(**vars(args))
     sub.dn_train, sub.dn_eval, sub.dn_steps = 64, 16, 3000
-    sub.dn_ref_spp, sub.dn_eval_ref_spp, sub.dn_spp_in, sub.dn_depth_in = 256, 1024, 4, 0
+    sub.dn_ref_spp, sub.dn_eval_ref_spp, sub.dn_spp_in, sub.dn_depth_in, sub.dn_rr_in = 256, 1024, 4, 0, -1
     sub.dn_res = sub.dn_train_res = 512
     line = run_denoise(sub)
     line.pop("per_room", None)
@@ -688,8 +704,9 @@ def run_denoise_infer(args):
             "roofline": {"bound": "tensor", "achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s",
                          "frac": round(achieved / peak, 5), "traffic": None, "peak_kind": peak_kind,
                          "algorithmic_flops_per_call": flops,
-                         "note": "whole forward pass timed (convolutions plus pooling, upsampling, concatenation"
-                                 " and packing kernels)"},
+                         "note": "whole forward pass timed: input packing and the 19 convolutions (on the tensor"
+                                 " cores the pooling, upsampling + concatenation, residual and output transform are"
+                                 " stores of their epilogues; on the CUDA cores kernels of their own)"},
             "clocks": clk}
     print(json.dumps(line), flush=True)
 

@@ -252,12 +252,9 @@ cudaError_t Denoiser::check(bool &ok) {
     return e;
 }
 
-cudaError_t Denoiser::conv_fwd(int ci, const Buf &in, __nv_bfloat16 *y, float *y32, cudaStream_t st) {
+cudaError_t Denoiser::tc_plan(int ci, const Buf &in, dn::TcConvPlan *&plan) {
     const Conv &c = convs_[ci];
     const int h = h_ >> in.level, w = w_dim_ >> in.level;
-    const float *bias = w_ + c.offset + (size_t)c.cout * 9 * c.cin;
-    if (!tensor_cores_)
-        return dn::conv3x3_forward(in.x, wb_ + c.offset, bias, y, y32, n_, h, w, c.cin, c.cout, c.relu, st);
     const __nv_bfloat16 *x = in.x;
     const int cin = pad16(c.cin);
     if (cin != c.cin) {
@@ -272,10 +269,25 @@ cudaError_t Denoiser::conv_fwd(int ci, const Buf &in, __nv_bfloat16 *y, float *y
             return e;
         }
     }
-    return dn::conv3x3_forward_tc(pl, wtc_ + tc_off_[ci], bias, y, y32, partial_, err_, st);
+    plan = &pl;
+    return cudaSuccess;
 }
 
-cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h, int w, cudaStream_t st) {
+cudaError_t Denoiser::conv_fwd(int ci, const Buf &in, __nv_bfloat16 *y, float *y32, cudaStream_t st,
+                               const dn::TcFuse *fuse, bool overlap) {
+    const Conv &c = convs_[ci];
+    const int h = h_ >> in.level, w = w_dim_ >> in.level;
+    const float *bias = w_ + c.offset + (size_t)c.cout * 9 * c.cin;
+    if (!tensor_cores_)
+        return dn::conv3x3_forward(in.x, wb_ + c.offset, bias, y, y32, n_, h, w, c.cin, c.cout, c.relu, st);
+    dn::TcConvPlan *pl = nullptr;
+    cudaError_t e = tc_plan(ci, in, pl);
+    if (e != cudaSuccess) return e;
+    return dn::conv3x3_forward_tc(*pl, wtc_ + tc_off_[ci], bias, y, y32, partial_, err_, st, fuse, overlap);
+}
+
+cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h, int w, cudaStream_t st,
+                              float *out_rad) {
     if (h % 16 || w % 16 || n <= 0) return cudaErrorInvalidValue;
     cudaError_t e = ensure(n, h, w);
     if (e != cudaSuccess) return e;
@@ -283,18 +295,40 @@ cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h
     auto chk = [&](cudaError_t x) { if (x != cudaSuccess && e == cudaSuccess) e = x; };
     feat_ = feat;
     chk(dn::pack_input(rad, feat, act_[0].x, tensor_cores_ ? x16_ : nullptr, px, st));
+    // On the tensor cores the poolings and the upsampling + concatenations are
+    // stores of the convolutions' epilogues (dn::TcFuse): the second
+    // convolution of encoder level l < 4 also writes the pooled input of level
+    // l + 1 and its output into the skip channels of cat_l; the second
+    // convolution of level l > 0 (bottleneck, decoder) writes its output,
+    // upsampled, into the first channels of cat_{l-1}. For inference (out_rad)
+    // those convolutions' own outputs, which only the backward pass reads,
+    // are not stored, and each convolution's prologue overlaps the previous
+    // kernel (programmatic dependent launch; no kernel of the pass writes
+    // weights).
+    const bool fuse = tensor_cores_, infer = out_rad != nullptr;
+    const int kCat[4] = {24, 21, 18, 15};  // act_ index of cat_l (layout in ensure)
     int conv = 0;
     // encoder
     int idx = 1, prev = 0;
     for (int l = 0; l < 5; l++) {
         if (l > 0) {
             const Buf &src = act_[prev];
-            chk(dn::avgpool(src.x, act_[idx].x, n, h >> (l - 1), w >> (l - 1), src.c, st));
+            if (!fuse) chk(dn::avgpool(src.x, act_[idx].x, n, h >> (l - 1), w >> (l - 1), src.c, st));
             prev = idx++;
         }
-        chk(conv_fwd(conv++, act_[prev], act_[idx].x, nullptr, st));
+        chk(conv_fwd(conv++, act_[prev], act_[idx].x, nullptr, st, nullptr, infer));
         prev = idx++;
-        chk(conv_fwd(conv++, act_[prev], act_[idx].x, nullptr, st));
+        dn::TcFuse f;
+        const Buf &cat = act_[kCat[l < 4 ? l : 3]];
+        f.cat = cat.x, f.cat_c = cat.c;
+        if (l < 4) {
+            f.pool = act_[idx + 1].x;
+            f.cat_off = cat.c - kEnc[l];
+        } else {
+            f.cat_up = 1;
+        }
+        chk(conv_fwd(conv++, act_[prev], fuse && infer ? nullptr : act_[idx].x, nullptr, st, fuse ? &f : nullptr,
+                     infer));
         prev = idx++;
     }
     // decoder: prev = e4 (index 14)
@@ -304,17 +338,37 @@ cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h
         Buf &cat = act_[idx];
         const Buf &low = act_[prev];
         const Buf &skip = act_[skip_idx[k]];
-        chk(dn::upsample_concat(low.x, skip.x, cat.x, n, h >> (l + 1), w >> (l + 1), low.c, skip.c, st));
+        if (!fuse)
+            chk(dn::upsample_concat(low.x, skip.x, cat.x, n, h >> (l + 1), w >> (l + 1), low.c, skip.c, st));
         prev = idx++;
-        chk(conv_fwd(conv++, act_[prev], act_[idx].x, nullptr, st));
+        chk(conv_fwd(conv++, act_[prev], act_[idx].x, nullptr, st, nullptr, infer));
         prev = idx++;
-        chk(conv_fwd(conv++, act_[prev], act_[idx].x, nullptr, st));
+        dn::TcFuse f;
+        const bool up = fuse && l > 0;
+        if (up) f.cat = act_[kCat[l - 1]].x, f.cat_c = act_[kCat[l - 1]].c, f.cat_up = 1;
+        chk(conv_fwd(conv++, act_[prev], up && infer ? nullptr : act_[idx].x, nullptr, st, up ? &f : nullptr,
+                     infer));
         prev = idx++;
     }
-    // output convolution (no ReLU), FP32
-    chk(conv_fwd(conv, act_[prev], nullptr, out_, st));
-    // the network predicts a correction to the noisy input's log radiance
-    chk(dn::add_input(out_, act_[0].x, px, st));
+    // output convolution (no ReLU), FP32; the network predicts a correction
+    // to the noisy input's log radiance (residual), and the output transform
+    // gives radiance: both in its epilogue unless it splits its taps
+    dn::TcConvPlan *pl = nullptr;
+    bool fused_out = false;
+    if (fuse && e == cudaSuccess) {
+        chk(tc_plan(conv, act_[prev], pl));
+        fused_out = pl && pl->splits == 1;
+    }
+    if (fused_out) {
+        dn::TcFuse f;
+        f.res = act_[0].x, f.res_c = act_[0].c;
+        f.rad = out_rad, f.feat = feat;
+        chk(conv_fwd(conv, act_[prev], nullptr, out_, st, &f, infer));
+    } else {
+        chk(conv_fwd(conv, act_[prev], nullptr, out_, st));
+        chk(dn::add_input(out_, act_[0].x, px, st));
+        if (infer) chk(output_radiance(out_rad, st));
+    }
     return e;
 }
 
@@ -432,8 +486,7 @@ cudaError_t Denoiser::denoise(const float *rad, const __half *feat, int n, int h
     if (graph_ && key == graph_key_) return cudaGraphLaunch(graph_, st);
     // new buffers or sizes: run on the stream (allocating and planning as
     // needed), then record the same launches for the calls that follow
-    cudaError_t e = forward(rad, feat, n, h, w, st);
-    if (e == cudaSuccess) e = output_radiance(out, st);
+    cudaError_t e = forward(rad, feat, n, h, w, st, out);
     if (e != cudaSuccess) return e;
     if (graph_) cudaGraphExecDestroy(graph_);
     graph_ = nullptr;
@@ -442,8 +495,7 @@ cudaError_t Denoiser::denoise(const float *rad, const __half *feat, int n, int h
         return e;
     }
     if ((e = cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
-    cudaError_t le = forward(rad, feat, n, h, w, capture_stream_);
-    if (le == cudaSuccess) le = output_radiance(out, capture_stream_);
+    cudaError_t le = forward(rad, feat, n, h, w, capture_stream_, out);
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(capture_stream_, &g);
     if (le == cudaSuccess && e == cudaSuccess) e = cudaGraphInstantiate(&graph_, g, 0);

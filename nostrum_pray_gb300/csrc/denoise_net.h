@@ -24,7 +24,10 @@ class Denoiser {
     // radiance: n*h*w*3 floats, feat: n*h*w*7 halves (albedo, normal, depth);
     // h and w multiples of 16. The network output stays on the device; feat
     // must stay valid through the backward / output_radiance that follow.
-    cudaError_t forward(const float *rad, const __half *feat, int n, int h, int w, cudaStream_t st);
+    // With out_rad (inference) the denoised radiance also goes there, and the
+    // activations that only the backward pass reads may not be stored.
+    cudaError_t forward(const float *rad, const __half *feat, int n, int h, int w, cudaStream_t st,
+                        float *out_rad = nullptr);
     // after forward: L1 loss against the target radiance, all gradients
     cudaError_t backward(const float *target, cudaStream_t st);
     cudaError_t apply_adam(float lr, cudaStream_t st);
@@ -55,7 +58,10 @@ class Denoiser {
     template <class T>
     cudaError_t take(T *&p, size_t n);
     cudaError_t ensure(int n, int h, int w);
-    cudaError_t conv_fwd(int ci, const Buf &in, __nv_bfloat16 *y, float *y32, cudaStream_t st);
+    cudaError_t conv_fwd(int ci, const Buf &in, __nv_bfloat16 *y, float *y32, cudaStream_t st,
+                         const dn::TcFuse *fuse = nullptr, bool overlap = false);
+    // the tensor-core plan of convolution ci on input `in` (made on first use)
+    cudaError_t tc_plan(int ci, const Buf &in, dn::TcConvPlan *&plan);
     // packed BF16 weights of the tensor-core kernel, from the FP32 master copy
     cudaError_t refresh_tc_weights(cudaStream_t st);
     void release();

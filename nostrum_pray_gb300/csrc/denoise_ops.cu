@@ -310,6 +310,9 @@ __device__ __forceinline__ float demod(const __half *feat, size_t i) {
 // x16 (optional) receives the same 10 channels padded to 16 with zeros
 __global__ void k_pack_input(const float *rad, const __half *feat, __nv_bfloat16 *x, __nv_bfloat16 *x16,
                              size_t pixels) {
+    // the first convolution may launch now (its prologue overlaps this
+    // kernel; it waits for this kernel's completion before reading x16)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     for (size_t p = gtid(); p < pixels; p += gstride()) {
         __nv_bfloat16 v[16];
         for (int k = 0; k < 3; k++) v[k] = __float2bfloat16(log1pf(fmaxf(rad[3 * p + k], 0.f) / demod(feat, 3 * p + k)));

@@ -52,8 +52,36 @@ struct TcPackJob {
     int cin_f, cout_f, cin_pad, npad, bwd;
 };
 cudaError_t tc_pack_all(const TcPackJob *jobs_dev, int njobs, size_t total, cudaStream_t st);
+// Extra stores of a forward convolution's epilogue, so that the network's
+// pooling, upsampling + concatenation, residual and output transform need no
+// kernels of their own. Each takes the values exactly as the separate kernel
+// would (the BF16-rounded outputs; the FP32 output plus the residual), so the
+// results are the same bits.
+//   pool: the 2 x 2 average of the BF16 outputs, (h / 2) x (w / 2) x cout;
+//   cat:  the BF16 outputs also into channels [cat_off, cat_off + cout) of a
+//         cat_c-channel tensor, at the same pixel (cat_up 0) or, nearest 2x
+//         upsampling, at the 2 x 2 block of a 2h x 2w tensor (cat_up 1);
+//   res:  FP32 output += res[pixel * res_c + channel] (BF16);
+//   rad:  (cout 3) rad = expm1(FP32 output) * (max(albedo, 0) + kDemodFloor),
+//         the albedo from feat (7 halves per pixel).
+// pool and cat need cout a multiple of 16, res and rad the FP32 output; none
+// works with a tap split (p.splits > 1).
+struct TcFuse {
+    __nv_bfloat16 *pool = nullptr;
+    __nv_bfloat16 *cat = nullptr;
+    int cat_c = 0, cat_off = 0, cat_up = 0;
+    const __nv_bfloat16 *res = nullptr;
+    int res_c = 0;
+    float *rad = nullptr;
+    const __half *feat = nullptr;
+};
 cudaError_t conv3x3_forward_tc(const TcConvPlan &p, const __nv_bfloat16 *wpacked, const float *bias,
-                               __nv_bfloat16 *y, float *y32, float *partial, int *err, cudaStream_t st);
+                               __nv_bfloat16 *y, float *y32, float *partial, int *err, cudaStream_t st,
+                               const TcFuse *fuse = nullptr, bool overlap_prologue = false);
+// overlap_prologue: launch with programmatic stream serialisation, so that the
+// kernel's prologue (barriers, tensor memory, weight copies) overlaps the
+// previous kernel of the stream; its input copies wait for that kernel to
+// complete. The previous kernel must not write the weights or the bias.
 // Weight gradient of a 3x3 convolution on the tensor cores:
 // dw[co][tap][ci] += sum over pixels p of g[p][co] * x[p + offset(tap)][ci],
 // a GEMM with M = output channels (padded to 128), N = input channels, K =

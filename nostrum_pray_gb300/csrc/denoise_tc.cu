@@ -18,9 +18,15 @@
 // when they fit or through a ring of per-tap stages. One thread issues the
 // kind::f16 MMAs (M 128, N Npad, K 16) and commits them to mbarriers.
 //
-// The deep, small levels have too few tiles for 152 SMs: there the nine taps
-// are split over 3 or 9 CTAs per tile, each writing FP32 partial sums that a
-// second kernel adds in split order (deterministic) with the bias and ReLU.
+// The deep, small levels have too few tiles for 152 SMs: there each tile's
+// output channels are split over CTAs (each loads its slice of the weights
+// with one 3-D TMA box), or, for a single 16-channel chunk, the nine taps over
+// 3 or 9 CTAs, each writing FP32 partial sums that a second kernel adds in
+// split order (deterministic) with the bias and ReLU.
+//
+// The epilogue also performs the network's glue (TcFuse): 2 x 2 average
+// pooling, nearest 2x upsampling into a concatenation, the residual add and
+// the output transform, as extra stores of the values it holds.
 //
 // Every mbarrier wait is bounded: on timeout the kernel records an error,
 // stops issuing, waits (bounded) for the copies and MMAs it issued, and frees
@@ -69,9 +75,24 @@ struct TcArgs {
     uint32_t w_off, bar_off;  // shared-memory offsets (the halo is at 0)
     uint32_t halo_stride;     // persistent kernel: distance between the halo ring's slots
     int *err;
+    TcFuse f;                 // extra stores of the epilogue
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Programmatic dependent launch. A convolution launched with programmatic
+// stream serialisation may start while the previous kernel of the stream
+// still runs: its prologue (barriers, tensor memory, weight copies) overlaps
+// that kernel's tail, and the thread that loads the input waits here for the
+// previous kernel to complete (and its writes to be visible) before the first
+// input copy. Every global store of the kernel follows that wait (the
+// epilogue runs after the MMAs, which follow the input copies). Once past it,
+// the CTA lets the next kernel launch. Launched without the attribute, both
+// instructions return at once.
+__device__ __forceinline__ void grid_dependency_wait() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
 
 // Shared-memory matrix descriptor: start, leading (K-direction) and stride
 // (8-row group) byte offsets, descriptor version 1, no swizzle.
@@ -154,14 +175,19 @@ __device__ __forceinline__ uint32_t pack2(float a, float b) {
 // Epilogue of one tile: the calling warp reads TMEM lanes 32q..32q+31 (q =
 // quad, the warp's lane quadrant: its warp index mod 4; tile rows m = pixel
 // (m / 8, m % 8)) from column `tmem` on, 16 columns at a time, and stores
-// bias + ReLU + BF16 (16-byte stores), FP32, or raw FP32 partials.
+// bias + ReLU + BF16 (16-byte stores), FP32, or raw FP32 partials, plus the
+// extra stores of P.f. A warp holds four whole tile rows, so the 2 x 2 blocks
+// of the pooling are lanes (l, l + 1, l + 8, l + 9) for l with even row and
+// column, summed in the order of k_avgpool (row-major).
 __device__ __forceinline__ void epilogue(const TcArgs &P, uint32_t tmem, int img, int y0, int x0, int split,
                                          int quad, int n0 = 0) {
-    const int m = quad * 32 + (int)(threadIdx.x & 31);
+    const int lane = (int)(threadIdx.x & 31);
+    const int m = quad * 32 + lane;
     const int yy = y0 + (m >> 3), xx = x0 + (m & 7);
     const bool valid = yy < P.h && xx < P.wd;
     const size_t M = (size_t)P.n * P.h * P.wd;
     const size_t pix = ((size_t)img * P.h + yy) * P.wd + xx;
+    const bool vec = (P.y || P.f.pool || P.f.cat) && (P.cout & 15) == 0;
     for (int c0 = 0; c0 < P.npad; c0 += 16) {
         uint32_t r[16];
         const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0;
@@ -174,23 +200,64 @@ __device__ __forceinline__ void epilogue(const TcArgs &P, uint32_t tmem, int img
             : "r"(taddr)
             : "memory");
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (!valid) continue;
+        // the pooling's shuffles need every lane of the warp
+        if (!valid && !(vec && P.f.pool)) continue;
         if (P.partial) {
             float4 *o = reinterpret_cast<float4 *>(P.partial + ((size_t)split * M + pix) * P.npad + c0);
 #pragma unroll
             for (int k = 0; k < 4; k++)
                 o[k] = make_float4(__uint_as_float(r[4 * k]), __uint_as_float(r[4 * k + 1]),
                                    __uint_as_float(r[4 * k + 2]), __uint_as_float(r[4 * k + 3]));
-        } else if (P.y && (P.cout & 15) == 0) {
+        } else if (vec) {
             float v[16];
 #pragma unroll
             for (int k = 0; k < 16; k++) {
                 v[k] = __uint_as_float(r[k]) + __ldg(P.bias + n0 + c0 + k);
                 if (P.relu) v[k] = fmaxf(v[k], 0.f);
             }
-            uint4 *o = reinterpret_cast<uint4 *>(P.y + pix * P.cout + n0 + c0);
-            o[0] = make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
-            o[1] = make_uint4(pack2(v[8], v[9]), pack2(v[10], v[11]), pack2(v[12], v[13]), pack2(v[14], v[15]));
+            const uint4 lo = make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
+            const uint4 hi =
+                make_uint4(pack2(v[8], v[9]), pack2(v[10], v[11]), pack2(v[12], v[13]), pack2(v[14], v[15]));
+            if (valid && P.y) {
+                uint4 *o = reinterpret_cast<uint4 *>(P.y + pix * P.cout + n0 + c0);
+                o[0] = lo, o[1] = hi;
+            }
+            if (valid && P.f.cat) {
+                const int ch = P.f.cat_off + n0 + c0;
+                if (P.f.cat_up) {
+                    const size_t W2 = 2 * (size_t)P.wd;
+                    const size_t b = (((size_t)img * 2 * P.h + 2 * yy) * W2 + 2 * xx) * P.f.cat_c + ch;
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        uint4 *o = reinterpret_cast<uint4 *>(P.f.cat + b + ((q >> 1) * W2 + (q & 1)) * P.f.cat_c);
+                        o[0] = lo, o[1] = hi;
+                    }
+                } else {
+                    uint4 *o = reinterpret_cast<uint4 *>(P.f.cat + pix * P.f.cat_c + ch);
+                    o[0] = lo, o[1] = hi;
+                }
+            }
+            if (P.f.pool) {
+                const uint32_t wd[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+                uint32_t po[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    const __nv_bfloat162 a2 = *reinterpret_cast<const __nv_bfloat162 *>(&wd[k]);
+                    const float a0 = __low2float(a2), a1 = __high2float(a2);
+                    const float b0 = __shfl_down_sync(0xFFFFFFFFu, a0, 1), b1 = __shfl_down_sync(0xFFFFFFFFu, a1, 1);
+                    const float c0v = __shfl_down_sync(0xFFFFFFFFu, a0, 8);
+                    const float c1v = __shfl_down_sync(0xFFFFFFFFu, a1, 8);
+                    const float d0 = __shfl_down_sync(0xFFFFFFFFu, a0, 9), d1 = __shfl_down_sync(0xFFFFFFFFu, a1, 9);
+                    po[k] = pack2(0.25f * (a0 + b0 + c0v + d0), 0.25f * (a1 + b1 + c1v + d1));
+                }
+                const int ho = P.h >> 1, wo = P.wd >> 1, yo = yy >> 1, xo = xx >> 1;
+                if (((lane >> 3) & 1) == 0 && (lane & 1) == 0 && yo < ho && xo < wo) {
+                    uint4 *o = reinterpret_cast<uint4 *>(P.f.pool + (((size_t)img * ho + yo) * wo + xo) * P.cout +
+                                                         n0 + c0);
+                    o[0] = make_uint4(po[0], po[1], po[2], po[3]);
+                    o[1] = make_uint4(po[4], po[5], po[6], po[7]);
+                }
+            }
         } else {
 #pragma unroll
             for (int k = 0; k < 16; k++) {
@@ -199,7 +266,11 @@ __device__ __forceinline__ void epilogue(const TcArgs &P, uint32_t tmem, int img
                 float v = __uint_as_float(r[k]) + __ldg(P.bias + co);
                 if (P.relu) v = fmaxf(v, 0.f);
                 if (P.y) P.y[pix * P.cout + co] = __float2bfloat16(v);
+                if (P.f.res) v += __bfloat162float(P.f.res[pix * P.f.res_c + co]);
                 if (P.y32) P.y32[pix * P.cout + co] = v;
+                if (P.f.rad)
+                    P.f.rad[pix * 3 + co] =
+                        expm1f(v) * (fmaxf(__half2float(P.f.feat[7 * pix + co]), 0.f) + kDemodFloor);
             }
         }
     }
@@ -248,9 +319,6 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtenso
 
     if (tid == 0) {
         bool ok = true;
-        // halo: one copy per 8-channel chunk, all completing on bars[0]
-        mbar_expect_tx(bar(0), (uint32_t)nchunk * kChunkBytes);
-        for (int c = 0; c < nchunk; c++) tma_halo(halo + c * kPlaneBytes, &xmap, bar(0), 8 * c, x0 - 1, y0 - 1, img);
         // weights: the first `stages` loads; with the output-channel split, one
         // TMA box per load: rows n0..n0+npad of every (tap, chunk) of the stage
         int issued = 0;
@@ -265,6 +333,11 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __grid_constant__ CUtenso
                           stage_bytes, bar(2 + stage));
         };
         for (; issued < nloads && issued < P.stages; issued++) load_weights(issued, issued);
+        // the weights do not depend on the previous kernel; the input does
+        grid_dependency_wait();
+        // halo: one copy per 8-channel chunk, all completing on bars[0]
+        mbar_expect_tx(bar(0), (uint32_t)nchunk * kChunkBytes);
+        for (int c = 0; c < nchunk; c++) tma_halo(halo + c * kPlaneBytes, &xmap, bar(0), 8 * c, x0 - 1, y0 - 1, img);
         const bool halo_done = mbar_wait(bar(0), 0);
         ok = halo_done;
         const uint32_t idesc = inst_desc(128, P.npad);
@@ -403,6 +476,7 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_tc_persistent(const __grid_
         if (lane == 0 && items > 0) {
             mbar_expect_tx(bar(wbar), wbytes);
             bulk_copy(wbase, P.w, wbytes, bar(wbar));
+            grid_dependency_wait();
             for (int i = 0; i < items && !*abort_flag; i++) {
                 const int h = i % H;
                 if (i >= H && !mbar_wait(bar(empty0 + h), (uint32_t)((i / H) - 1) & 1)) {
@@ -1061,8 +1135,17 @@ cudaError_t tc_conv_plan(TcConvPlan &p, const __nv_bfloat16 *x, int n, int h, in
 }
 
 cudaError_t conv3x3_forward_tc(const TcConvPlan &p, const __nv_bfloat16 *wpacked, const float *bias,
-                               __nv_bfloat16 *y, float *y32, float *partial, int *err, cudaStream_t st) {
+                               __nv_bfloat16 *y, float *y32, float *partial, int *err, cudaStream_t st,
+                               const TcFuse *fuse, bool overlap_prologue) {
     if (p.splits > 1 && !partial) return cudaErrorInvalidValue;
+    if (fuse) {
+        if (p.splits > 1) return cudaErrorInvalidValue;
+        if ((fuse->pool || fuse->cat) && (p.cout & 15)) return cudaErrorInvalidValue;
+        if (fuse->cat && (fuse->cat_c & 7 || fuse->cat_off & 7 || fuse->cat_off + p.cout > fuse->cat_c))
+            return cudaErrorInvalidValue;
+        if ((fuse->res || fuse->rad) && !y32) return cudaErrorInvalidValue;
+        if (fuse->rad && (p.cout != 3 || !fuse->feat)) return cudaErrorInvalidValue;
+    }
     // the shared-memory opt-in is a per-device setting of each kernel: once per device
     static std::atomic<uint64_t> attr_set{0};
     int dev = 0;
@@ -1088,6 +1171,7 @@ cudaError_t conv3x3_forward_tc(const TcConvPlan &p, const __nv_bfloat16 *wpacked
     a.tmem_cols = p.tmem_cols;
     a.w_off = p.w_off, a.bar_off = p.bar_off, a.halo_stride = p.halo_stride;
     a.err = err;
+    if (fuse) a.f = *fuse;
     CUtensorMap map, wmap;
     std::memcpy(&map, p.tmap, sizeof(map));
     std::memset(&wmap, 0, sizeof(wmap));
@@ -1105,12 +1189,23 @@ cudaError_t conv3x3_forward_tc(const TcConvPlan &p, const __nv_bfloat16 *wpacked
                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
     }
-    if (p.persistent)
-        k_conv_tc_persistent<<<(unsigned)p.grid, kWsThreads, p.smem, st>>>(map, a);
-    else
-        k_conv_tc<<<dim3((unsigned)p.tiles, (unsigned)(p.nsplit > 1 ? p.nsplit : p.splits)), 128, p.smem, st>>>(
-            map, wmap, a);
-    cudaError_t e = cudaGetLastError();
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.dynamicSmemBytes = p.smem;
+    cfg.stream = st;
+    cfg.attrs = overlap_prologue ? attr : nullptr;
+    cfg.numAttrs = overlap_prologue ? 1 : 0;
+    cudaError_t e;
+    if (p.persistent) {
+        cfg.gridDim = dim3((unsigned)p.grid), cfg.blockDim = dim3(kWsThreads);
+        e = cudaLaunchKernelEx(&cfg, k_conv_tc_persistent, map, a);
+    } else {
+        cfg.gridDim = dim3((unsigned)p.tiles, (unsigned)(p.nsplit > 1 ? p.nsplit : p.splits)), cfg.blockDim = dim3(128);
+        e = cudaLaunchKernelEx(&cfg, k_conv_tc, map, wmap, a);
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess || p.splits == 1) return e;
     const size_t M = (size_t)p.n * p.h * p.w;
     if ((p.cout & 3) == 0)

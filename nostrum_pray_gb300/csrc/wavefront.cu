@@ -23,14 +23,18 @@
 // Built with --fmad=false like the rest of the tracing code.
 #include <cfloat>
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "../../include/nostrum_pray_sampling.h"
 #include "device_layout.h"
 #include "trace_launch.h"
 #include "traverse.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace pray_gpu {
 
@@ -338,24 +342,39 @@ __global__ void __launch_bounds__(kThreads) k_wf_finish(PtLaunch L, WavefrontScr
     }
 }
 
-// FP64 relative MSE in one block (deterministic order; the images are a few
-// million values, so one SM streams them in well under a millisecond).
-__global__ void __launch_bounds__(1024) k_relmse(const double *img, double a, const double *ref, double b,
-                                                 uint64_t n, double *out) {
-    __shared__ double sm[1024];
+// FP64 relative MSE over one cluster of CTAs, the whole grid (distributed
+// shared memory, no global scratch, one launch). The FP64 divide is many
+// instructions on this part's narrow FP64 pipe, so one SM would take
+// milliseconds for a 512^2 frame; 16 SMs share it (8 where a 16-CTA cluster
+// cannot be placed). Deterministic for a given cluster size: each CTA sums a
+// fixed stride of the values, reduces its threads' sums by a fixed tree, and
+// CTA 0 adds the CTAs' sums in rank order.
+constexpr int kRelmseThreads = 1024;
+
+__global__ void __launch_bounds__(kRelmseThreads) k_relmse(const double *img, double a, const double *ref, double b,
+                                                           uint64_t n, double *out) {
+    __shared__ double sm[kRelmseThreads];
+    cg::cluster_group cluster = cg::this_cluster();
+    const unsigned rank = cluster.block_rank(), ctas = cluster.num_blocks();
     double acc = 0.0;
-    for (uint64_t i = threadIdx.x; i < n; i += 1024) {
+    for (uint64_t i = (uint64_t)rank * kRelmseThreads + threadIdx.x; i < n; i += (uint64_t)kRelmseThreads * ctas) {
         const double x = img[i] * a, r = ref[i] * b;
         const double d = x - r;
         acc += d * d / (r * r + 0.01);
     }
     sm[threadIdx.x] = acc;
     __syncthreads();
-    for (int o = 512; o > 0; o >>= 1) {
+    for (int o = kRelmseThreads / 2; o > 0; o >>= 1) {
         if ((int)threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
         __syncthreads();
     }
-    if (threadIdx.x == 0) out[0] = n ? sm[0] / (double)n : 0.0;
+    cluster.sync();  // every CTA's sum in its sm[0]
+    if (rank == 0 && threadIdx.x == 0) {
+        double total = 0.0;
+        for (unsigned c = 0; c < ctas; c++) total += *cluster.map_shared_rank(&sm[0], c);
+        out[0] = n ? total / (double)n : 0.0;
+    }
+    cluster.sync();  // the other CTAs' shared memory stays until CTA 0 has read it
 }
 
 }  // namespace
@@ -432,8 +451,35 @@ cudaError_t record_wavefront_frame(const DevScene &s, const PtLaunch &L, const W
 
 cudaError_t launch_relmse(const double *img, double a, const double *ref, double b, uint64_t n, double *out,
                           cudaStream_t stream) {
-    k_relmse<<<1, 1024, 0, stream>>>(img, a, ref, b, n, out);
-    return cudaGetLastError();
+    // the cluster size, once per device: 16 (a non-portable size) when the
+    // occupancy query can place such a cluster, else 8
+    static std::atomic<int> sizes[64];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.y = 1, attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(kRelmseThreads), cfg.stream = stream;
+    cfg.attrs = attr, cfg.numAttrs = 1;
+    int ctas = sizes[dev].load();
+    if (ctas == 0) {
+        ctas = 8;
+        if (cudaFuncSetAttribute(k_relmse, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+            int clusters = 0;
+            attr[0].val.clusterDim.x = 16;
+            cfg.gridDim = dim3(16);
+            if (cudaOccupancyMaxActiveClusters(&clusters, k_relmse, &cfg) == cudaSuccess && clusters >= 1) ctas = 16;
+        }
+        cudaGetLastError();  // a refused query leaves the 8-CTA cluster
+        sizes[dev].store(ctas);
+    }
+    attr[0].val.clusterDim.x = (unsigned)ctas;
+    cfg.gridDim = dim3((unsigned)ctas);
+    e = cudaLaunchKernelEx(&cfg, k_relmse, img, a, ref, b, n, out);
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 }  // namespace pray_gpu

@@ -40,6 +40,7 @@ class DenoiseConfig:
     spp_ref: int = 1024
     depth: int = 8
     depth_in: int = 0        # path depth of the noisy input (0: depth); references and plain renders use depth
+    rr_in: int = -1          # Russian roulette from this depth in the noisy input (-1: rr_depth); unbiased
     rr_depth: int = 3
     train_rooms: int = 96
     eval_rooms: int = 16
@@ -68,18 +69,25 @@ def forward_flops(h: int, w: int, n: int = 1) -> int:
 
 
 def denoise_launches(h: int, w: int, n: int = 1, sm_count: int = 152, tensor_cores: bool = True) -> int:
-    """Kernels one pray_denoise call launches: input packing, 4 poolings, 4
-    upsample-concatenations, the 19 convolutions, the residual add and the
-    output transform. On the tensor cores a convolution with fewer than two
-    16x8-pixel tiles per SM splits its output channels over CTAs, or, with
-    a single 16-channel chunk, its taps, which adds a finalize kernel (the
-    rule of tc_conv_plan in csrc/denoise_tc.cu)."""
-    convs = 0
+    """Kernels one pray_denoise call launches. On the CUDA cores: input
+    packing, 4 poolings, 4 upsample-concatenations, the 19 convolutions, the
+    residual add and the output transform. On the tensor cores the poolings,
+    concatenations, residual and output transform are stores of the
+    convolutions' epilogues: input packing and the 19 convolutions. There a
+    convolution with fewer than two 16x8-pixel tiles per SM splits its output
+    channels over CTAs, or, with a single 16-channel chunk, its taps, which
+    adds a finalize kernel (the rule of tc_conv_plan in
+    csrc/denoise_tc.cu); the output convolution split so keeps the residual
+    and output kernels."""
+    convs, split = 0, False
     for _, co, l in CONVS:
         tiles = n * -(-(w >> l) // 8) * -(-(h >> l) // 16)
         npad = -(-co // 16) * 16
-        convs += 2 if tensor_cores and tiles < 2 * sm_count and npad < 32 else 1
-    return 1 + 4 + 4 + convs + 2
+        split = tensor_cores and tiles < 2 * sm_count and npad < 32
+        convs += 2 if split else 1
+    if not tensor_cores:
+        return 1 + 4 + 4 + convs + 2
+    return 1 + convs + (2 if split else 0)
 
 
 def _setup(cfg: DenoiseConfig, res: Optional[int] = None):
@@ -87,17 +95,20 @@ def _setup(cfg: DenoiseConfig, res: Optional[int] = None):
     return scenes.room_setup(r, r, spp=cfg.spp_in, max_depth=cfg.depth)
 
 
-def _params(cfg, st, spp, seed, offset=0, depth=None):
+def _params(cfg, st, spp, seed, offset=0, depth=None, rr_depth=None):
     return native.pt_params(st, spp=spp, max_depth=cfg.depth if depth is None else depth, seed=seed,
-                            mode=native.PT_NEE, rr_depth=cfg.rr_depth, scheduler=native.SCHED_AUTO,
-                            sample_offset=offset)
+                            mode=native.PT_NEE, rr_depth=cfg.rr_depth if rr_depth is None else rr_depth,
+                            scheduler=native.SCHED_AUTO, sample_offset=offset)
 
 
 def input_params(cfg, st, seed):
     """The noisy input's render: spp_in samples per pixel, paths cut at
     depth_in bounces when it is set (the network then also restores the light
-    of the longer paths, which the references and plain renders keep)."""
-    return _params(cfg, st, cfg.spp_in, seed, depth=cfg.depth_in or cfg.depth)
+    of the longer paths, which the references and plain renders keep), and
+    Russian roulette from depth rr_in when it is set (an unbiased way to
+    shorten the input's paths: it trades their length for variance)."""
+    return _params(cfg, st, cfg.spp_in, seed, depth=cfg.depth_in or cfg.depth,
+                   rr_depth=cfg.rr_in if cfg.rr_in >= 0 else None)
 
 
 def render_room(cfg: DenoiseConfig, room_seed: int, torch, res: Optional[int] = None):
@@ -265,18 +276,25 @@ def denoised_eval(cfg: DenoiseConfig, den, sc, ref, room_seed: int, torch):
         main.wait_stream(side)
         den.denoise(rad, feat, out)
 
+    def run_with_prediction():
+        # the fallback decision: a second independent input, denoised, and
+        # half the relMSE between the two outputs read back to the host
+        run()
+        sc.render_pt(p2, None, rad2[0])
+        den.denoise(rad2, feat, out2)
+        return 0.5 * relmse(out[0], out2[0].to(torch.float64), torch)
+
     run()
     t = timed(run, torch)
     t_render = timed(lambda: sc.render_pt(p, None, rad[0]), torch)
     t_infer = timed(lambda: den.denoise(rad, feat, out), torch)
-    run()
+    run_with_prediction()
+    t_pred = timed(run_with_prediction, torch)
+    pred = run_with_prediction()
     e = relmse(out[0], ref, torch)
     e_noisy = relmse(rad[0], ref, torch)
-    sc.render_pt(p2, None, rad2[0])
-    den.denoise(rad2, feat, out2)
-    pred = 0.5 * relmse(out[0], out2[0].to(torch.float64), torch)
     return {"relmse_denoised": e, "relmse_noisy": e_noisy, "time_s": t, "render_s": t_render,
-            "inference_s": t_infer, "predicted": pred}
+            "inference_s": t_infer, "predicted": pred, "time_with_prediction_s": t_pred}
 
 
 def evaluate(cfg: DenoiseConfig, den, eval_rooms, torch, fallback_spp: int) -> Dict:
@@ -299,7 +317,8 @@ def evaluate(cfg: DenoiseConfig, den, eval_rooms, torch, fallback_spp: int) -> D
                 t_final = d["time_s"] + fb[0][2]
                 e_final = fb[0][1]
         rows.append({"seed": seed, "spp_plain_to_target": spp_plain, "time_plain_s": t_plain, **d,
-                     "fallback": used_fallback, "time_final_s": t_final, "relmse_final": e_final})
+                     "fallback": used_fallback, "time_final_s": t_final, "relmse_final": e_final,
+                     "time_final_with_prediction_s": t_final - d["time_s"] + d["time_with_prediction_s"]})
     return {"rooms": rows}
 
 

@@ -323,10 +323,15 @@ class Scene:
                                    _stream(stream)))
 
     # -- host-memory entry points -------------------------------------------
-    def render_rt_host(self, setup) -> Tuple[np.ndarray, np.ndarray]:
-        """Returns (image uint8 (height, width, 3), [primary rays, shadow rays])."""
+    def render_rt_host(self, setup, out: Optional[np.ndarray] = None) -> Tuple[np.ndarray, np.ndarray]:
+        """Returns (image uint8 (height, width, 3), [primary rays, shadow rays]);
+        `out`: a C-contiguous uint8 host array of that shape to write the
+        image into (a frame loop reuses one, pinned for the fastest copy)."""
         p, keep = rt_params(setup)
-        img = np.empty((setup.height, setup.width, 3), np.uint8)
+        shape = (setup.height, setup.width, 3)
+        if out is not None and (out.shape != shape or out.dtype != np.uint8 or not out.flags.c_contiguous):
+            raise PrayError(f"out must be a C-contiguous uint8 array of shape {shape}")
+        img = np.empty(shape, np.uint8) if out is None else out
         rays = np.zeros(2, np.uint64)
         check(lib().pray_render_rt_host(self._h, ctypes.byref(p), img.ctypes.data, rays.ctypes.data))
         del keep
@@ -341,10 +346,17 @@ class Scene:
         del keep
         return out
 
-    def render_pt_host(self, params: PtParams, radiance: bool = True):
-        """Returns (image uint8, mean radiance float32 or None, [paths, segments])."""
-        img = np.empty((params.height, params.width, 3), np.uint8)
-        rad = np.empty((params.height, params.width, 3), np.float32) if radiance else None
+    def render_pt_host(self, params: PtParams, radiance: bool = True, out: Optional[np.ndarray] = None,
+                       out_radiance: Optional[np.ndarray] = None):
+        """Returns (image uint8, mean radiance float32 or None, [paths, segments]);
+        `out` / `out_radiance`: C-contiguous host arrays of shape (height,
+        width, 3) to write into (uint8 / float32)."""
+        shape = (params.height, params.width, 3)
+        for a, dt in ((out, np.uint8), (out_radiance, np.float32)):
+            if a is not None and (a.shape != shape or a.dtype != dt or not a.flags.c_contiguous):
+                raise PrayError(f"output arrays must be C-contiguous {shape} arrays")
+        img = np.empty(shape, np.uint8) if out is None else out
+        rad = (np.empty(shape, np.float32) if out_radiance is None else out_radiance) if radiance else None
         rays = np.zeros(2, np.uint64)
         check(lib().pray_render_pt_host(self._h, ctypes.byref(params), img.ctypes.data, _ptr(rad),
                                         rays.ctypes.data))

@@ -131,16 +131,23 @@ def test_fp64_accumulation_in_chunks(oracle, scheduler):
     np.testing.assert_array_equal(acc.cpu().numpy(), want)
 
 
-def test_relmse_reduction():
-    rng = np.random.default_rng(0)
-    a = rng.random(30_001) * 2
-    r = rng.random(30_001)
+@pytest.mark.parametrize("n", [1, 5, 30_001, 512 * 512 * 3])
+def test_relmse_reduction(n):
+    """FP64 relMSE over one cluster of CTAs: fewer values than threads, a
+    ragged size and a 512^2 frame; the same bits on every call."""
+    rng = np.random.default_rng(n)
+    a = rng.random(n) * 2
+    r = rng.random(n)
     want = np.mean((a * 0.5 - r * 2.0) ** 2 / ((r * 2.0) ** 2 + 0.01))
     ta, tr = torch.from_numpy(a).cuda(), torch.from_numpy(r).cuda()
-    out = torch.zeros(1, dtype=torch.float64, device="cuda")
-    native.relmse(ta, 0.5, tr, 2.0, out)
-    torch.cuda.synchronize()
-    assert abs(out.item() - want) <= 1e-12 * max(1.0, want)
+    got = []
+    for _ in range(3):
+        out = torch.zeros(1, dtype=torch.float64, device="cuda")
+        native.relmse(ta, 0.5, tr, 2.0, out)
+        torch.cuda.synchronize()
+        got.append(out.item())
+    assert abs(got[0] - want) <= 1e-12 * max(1.0, want)
+    assert got[1] == got[0] and got[2] == got[0]
 
 
 @pytest.mark.parametrize("depth,n", [(0, 4), (1, 8), (2, 5)])
