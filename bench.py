@@ -685,9 +685,17 @@ def run_denoise_infer(args):
     e2e_ms = _timed_frames(e2e_step, args.steps, args.warmup, flush)
     stream.synchronize()
     flops = D.forward_flops(res, res, nb)
+    nbytes = D.forward_bytes(res, res, nb)
     per = ms / args.steps / 1e3
     peak, peak_kind = measured_bf16()
+    hbm, hbm_kind = measured_peaks()
     achieved = flops / per / 1e12
+    # the pass's arithmetic intensity (FLOPs per algorithmic DRAM byte) is
+    # below the machine's ridge point (bf16 peak / HBM bandwidth), so the
+    # memory roofline binds; the tensor-core figure is reported beside it
+    intensity = flops / nbytes
+    ridge = peak * 1e12 / (hbm * 1e9)
+    gbs = nbytes / per / 1e9
     line = {"metric": "denoised frames/s", "value": round(nb * args.steps / (ms / 1e3), 2), "unit": "frames/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
@@ -701,9 +709,15 @@ def run_denoise_infer(args):
             "gpu_launches": D.denoise_launches(res, res, nb, tensor_cores=not args.dn_cuda_cores,
                                                sm_count=torch.cuda.get_device_properties(0).multi_processor_count)
             * args.steps,
-            "roofline": {"bound": "tensor", "achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s",
-                         "frac": round(achieved / peak, 5), "traffic": None, "peak_kind": peak_kind,
-                         "algorithmic_flops_per_call": flops,
+            "roofline": ({"bound": "hbm", "achieved": round(gbs, 1), "peak": hbm, "unit": "GB/s",
+                          "frac": round(gbs / hbm, 4), "peak_kind": f"{hbm_kind} HBM copy bandwidth"}
+                         if intensity < ridge else
+                         {"bound": "tensor", "achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s",
+                          "frac": round(achieved / peak, 5), "peak_kind": peak_kind})
+                        | {"traffic": None, "algorithmic_bytes_per_call": nbytes, "algorithmic_flops_per_call": flops,
+                           "intensity_flop_per_byte": round(intensity, 1), "ridge_flop_per_byte": round(ridge, 1),
+                           "tensor": {"achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s",
+                                      "frac": round(achieved / peak, 5), "peak_kind": peak_kind},
                          "note": "whole forward pass timed: input packing and the 19 convolutions (on the tensor"
                                  " cores the pooling, upsampling + concatenation, residual and output transform are"
                                  " stores of their epilogues; on the CUDA cores kernels of their own)"},

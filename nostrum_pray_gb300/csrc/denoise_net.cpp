@@ -294,7 +294,12 @@ cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h
     const size_t px = (size_t)n * h * w;
     auto chk = [&](cudaError_t x) { if (x != cudaSuccess && e == cudaSuccess) e = x; };
     feat_ = feat;
-    chk(dn::pack_input(rad, feat, act_[0].x, tensor_cores_ ? x16_ : nullptr, px, st));
+    // the tensor cores read the input padded to 16 channels (x16_), also for
+    // the residual and the first convolution's weight gradient: the
+    // 10-channel copy is written only for the CUDA cores
+    chk(dn::pack_input(rad, feat, tensor_cores_ ? nullptr : act_[0].x, tensor_cores_ ? x16_ : nullptr, px, st));
+    const __nv_bfloat16 *x0 = tensor_cores_ ? x16_ : act_[0].x;
+    const int x0_c = tensor_cores_ ? pad16(kConvs[0][0]) : act_[0].c;
     // On the tensor cores the poolings and the upsampling + concatenations are
     // stores of the convolutions' epilogues (dn::TcFuse): the second
     // convolution of encoder level l < 4 also writes the pooled input of level
@@ -361,12 +366,12 @@ cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h
     }
     if (fused_out) {
         dn::TcFuse f;
-        f.res = act_[0].x, f.res_c = act_[0].c;
+        f.res = x0, f.res_c = x0_c;
         f.rad = out_rad, f.feat = feat;
         chk(conv_fwd(conv, act_[prev], nullptr, out_, st, &f, infer));
     } else {
         chk(conv_fwd(conv, act_[prev], nullptr, out_, st));
-        chk(dn::add_input(out_, act_[0].x, px, st));
+        chk(dn::add_input(out_, x0, x0_c, px, st));
         if (infer) chk(output_radiance(out_rad, st));
     }
     return e;

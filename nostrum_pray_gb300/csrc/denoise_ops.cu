@@ -318,7 +318,8 @@ __global__ void k_pack_input(const float *rad, const __half *feat, __nv_bfloat16
         for (int k = 0; k < 3; k++) v[k] = __float2bfloat16(log1pf(fmaxf(rad[3 * p + k], 0.f) / demod(feat, 3 * p + k)));
         for (int k = 0; k < 7; k++) v[3 + k] = __float2bfloat16(__half2float(feat[7 * p + k]));
         for (int k = 10; k < 16; k++) v[k] = __float2bfloat16(0.f);
-        for (int k = 0; k < 10; k++) x[p * 10 + k] = v[k];
+        if (x)
+            for (int k = 0; k < 10; k++) x[p * 10 + k] = v[k];
         if (x16) {
             uint4 *o = reinterpret_cast<uint4 *>(x16 + p * 16);
             o[0] = *reinterpret_cast<const uint4 *>(v);
@@ -343,8 +344,8 @@ __global__ void k_l1(const float *out, const float *target, const __half *feat, 
 }
 
 // residual output: out (log space) += the input's log(1 + radiance) channels
-__global__ void k_add_input(float *out, const __nv_bfloat16 *x0, size_t pixels) {
-    for (size_t i = gtid(); i < pixels * 3; i += gstride()) out[i] += bf(x0[(i / 3) * 10 + i % 3]);
+__global__ void k_add_input(float *out, const __nv_bfloat16 *x0, int x0_c, size_t pixels) {
+    for (size_t i = gtid(); i < pixels * 3; i += gstride()) out[i] += bf(x0[(i / 3) * x0_c + i % 3]);
 }
 
 __global__ void k_expm1(const float *out, const __half *feat, float *rad, size_t n) {
@@ -480,8 +481,8 @@ cudaError_t l1_loss(const float *out, const float *target, const __half *feat, f
     k_l1<<<blocks_for(n), 256, 0, st>>>(out, target, feat, g, loss, n);
     return cudaGetLastError();
 }
-cudaError_t add_input(float *out, const __nv_bfloat16 *x0, size_t pixels, cudaStream_t st) {
-    k_add_input<<<blocks_for(pixels * 3), 256, 0, st>>>(out, x0, pixels);
+cudaError_t add_input(float *out, const __nv_bfloat16 *x0, int x0_c, size_t pixels, cudaStream_t st) {
+    k_add_input<<<blocks_for(pixels * 3), 256, 0, st>>>(out, x0, x0_c, pixels);
     return cudaGetLastError();
 }
 cudaError_t expm1_out(const float *out, const __half *feat, float *rad, size_t n, cudaStream_t st) {

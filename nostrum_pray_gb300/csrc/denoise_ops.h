@@ -129,7 +129,7 @@ cudaError_t split_add(const float *gy, float *gx, size_t pixels, int c, int cy, 
 // max(albedo, 0) + kDemodFloor (per channel) on the way in and in the loss's
 // target, multiplied back on the way out.
 constexpr float kDemodFloor = 0.05f;
-// x: 10 channels; x16 (may be NULL): the same padded to 16 channels
+// x (may be NULL): 10 channels; x16 (may be NULL): the same padded to 16 channels
 cudaError_t pack_input(const float *rad, const __half *feat, __nv_bfloat16 *x, __nv_bfloat16 *x16, size_t pixels,
                        cudaStream_t st);
 // cat = [nearest 2x upsampling of low (c channels, h x w), skip (cs channels)]
@@ -137,7 +137,8 @@ cudaError_t upsample_concat(const __nv_bfloat16 *low, const __nv_bfloat16 *skip,
                             int w, int c, int cs, cudaStream_t st);
 cudaError_t l1_loss(const float *out, const float *target, const __half *feat, float *g, float *loss, size_t n,
                     cudaStream_t st);
-cudaError_t add_input(float *out, const __nv_bfloat16 *x0, size_t pixels, cudaStream_t st);
+// out (3 channels) += the first 3 of x0's x0_c channels (the input's log radiance)
+cudaError_t add_input(float *out, const __nv_bfloat16 *x0, int x0_c, size_t pixels, cudaStream_t st);
 cudaError_t expm1_out(const float *out, const __half *feat, float *rad, size_t n, cudaStream_t st);
 cudaError_t adam(float *w, const float *g, float *m, float *v, __nv_bfloat16 *wb, size_t n, float lr, float b1,
                  float b2, float eps, int step, cudaStream_t st);

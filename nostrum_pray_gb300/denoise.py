@@ -68,6 +68,36 @@ def forward_flops(h: int, w: int, n: int = 1) -> int:
     return n * sum(2 * 9 * ci * co * (h >> l) * (w >> l) for ci, co, l in CONVS)
 
 
+def forward_bytes(h: int, w: int, n: int = 1) -> int:
+    """Algorithmic DRAM bytes of one inference forward pass on the tensor
+    cores: every tensor read once and written once (halo re-reads excluded),
+    BF16 activations. Input packing reads the radiance (12 B per pixel) and
+    the features (14 B) and writes the 16-channel input; each convolution
+    reads its input (channels padded to 16) and writes, by the fused
+    epilogues: the encoder's second convolutions of levels 0-3 the pooled
+    tensor and the skip channels of the concatenation (not their own
+    output), the second convolutions of levels 4-1 their output upsampled
+    into the next concatenation (4 pixels each), the output convolution the
+    log-space and the final radiance (FP32) after reading 3 channels of the
+    input and the albedo; the others their output."""
+    px0 = n * h * w
+    total = px0 * (12 + 14 + 32)
+    for i, (ci, co, l) in enumerate(CONVS):
+        px = n * (h >> l) * (w >> l)
+        rd = 2 * (-(-ci // 16) * 16)
+        if i in (1, 3, 5, 7):
+            wr = 2 * co // 4 + 2 * co
+        elif i in (9, 11, 13, 15):
+            wr = 4 * 2 * co
+        elif i == len(CONVS) - 1:
+            rd += 6 + 6
+            wr = 12 + 12
+        else:
+            wr = 2 * co
+        total += px * (rd + wr)
+    return total
+
+
 def denoise_launches(h: int, w: int, n: int = 1, sm_count: int = 152, tensor_cores: bool = True) -> int:
     """Kernels one pray_denoise call launches. On the CUDA cores: input
     packing, 4 poolings, 4 upsample-concatenations, the 19 convolutions, the
