@@ -340,7 +340,9 @@ def run_ours(args):
         sub.steps, sub.warmup, sub.spp = max(3, min(args.steps, 10)), 3, 0
         sub.cpu_seconds = args.cpu_seconds / 2
         line["secondary"] = {}
-        for key, fn in (("room", run_pt), ("batch", run_batch), ("denoise", run_denoise_secondary)):
+        dn_fast = lambda a: run_denoise_secondary(a, spp_in=1, rr_in=0)
+        for key, fn in (("room", run_pt), ("batch", run_batch), ("denoise", dn_fast),
+                        ("denoise_4spp_input", run_denoise_secondary)):
             try:
                 line["secondary"][key] = fn(sub)
             except Exception as exc:  # a secondary workload must not cost the main line
@@ -624,17 +626,18 @@ def run_denoise(args):
     return line
 
 
-def run_denoise_secondary(args):
+def run_denoise_secondary(args, spp_in: int = 4, rr_in: int = -1):
     """The denoiser's time to relMSE <= 0.01, denoised / plain, at a reduced
     size for the default bench line: 64 training rooms with 256-spp targets,
-    3,000 Adam steps, 16 held-out rooms against 1,024-spp references, the
-    configured 4-spp input. The stated size (2,000 training rooms, 200
-    held-out rooms against 4,096-spp references) is `--workload denoise
-    --dn-train 2000 --dn-eval 200 --dn-steps 6000 --dn-ref-spp 256
-    --dn-eval-ref-spp 4096`."""
+    3,000 Adam steps, 16 held-out rooms against 1,024-spp references; the
+    input at spp_in samples per pixel (the configured 4, or 1 with Russian
+    roulette from the first bounce, rr_in 0). The stated size (2,000 training
+    rooms, 200 held-out rooms against 4,096-spp references) is `--workload
+    denoise --dn-train 2000 --dn-eval 200 --dn-steps 6000 --dn-ref-spp 256
+    --dn-eval-ref-spp 4096 --dn-spp-in 1 --dn-rr-in 0`."""
     sub = argparse.Namespace(**vars(args))
     sub.dn_train, sub.dn_eval, sub.dn_steps = 64, 16, 3000
-    sub.dn_ref_spp, sub.dn_eval_ref_spp, sub.dn_spp_in, sub.dn_depth_in, sub.dn_rr_in = 256, 1024, 4, 0, -1
+    sub.dn_ref_spp, sub.dn_eval_ref_spp, sub.dn_spp_in, sub.dn_depth_in, sub.dn_rr_in = 256, 1024, spp_in, 0, rr_in
     sub.dn_res = sub.dn_train_res = 512
     line = run_denoise(sub)
     line.pop("per_room", None)

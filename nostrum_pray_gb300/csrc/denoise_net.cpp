@@ -307,9 +307,10 @@ cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h
     // convolution of level l > 0 (bottleneck, decoder) writes its output,
     // upsampled, into the first channels of cat_{l-1}. For inference (out_rad)
     // those convolutions' own outputs, which only the backward pass reads,
-    // are not stored, and each convolution's prologue overlaps the previous
-    // kernel (programmatic dependent launch; no kernel of the pass writes
-    // weights).
+    // are not stored. Each convolution's prologue overlaps the previous
+    // kernel (programmatic dependent launch): the packed weights it loads
+    // there are written only by the packing after the optimizer step, which
+    // completes before input packing starts.
     const bool fuse = tensor_cores_, infer = out_rad != nullptr;
     const int kCat[4] = {24, 21, 18, 15};  // act_ index of cat_l (layout in ensure)
     int conv = 0;
@@ -321,7 +322,7 @@ cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h
             if (!fuse) chk(dn::avgpool(src.x, act_[idx].x, n, h >> (l - 1), w >> (l - 1), src.c, st));
             prev = idx++;
         }
-        chk(conv_fwd(conv++, act_[prev], act_[idx].x, nullptr, st, nullptr, infer));
+        chk(conv_fwd(conv++, act_[prev], act_[idx].x, nullptr, st, nullptr, fuse));
         prev = idx++;
         dn::TcFuse f;
         const Buf &cat = act_[kCat[l < 4 ? l : 3]];
@@ -333,7 +334,7 @@ cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h
             f.cat_up = 1;
         }
         chk(conv_fwd(conv++, act_[prev], fuse && infer ? nullptr : act_[idx].x, nullptr, st, fuse ? &f : nullptr,
-                     infer));
+                     fuse));
         prev = idx++;
     }
     // decoder: prev = e4 (index 14)
@@ -346,13 +347,13 @@ cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h
         if (!fuse)
             chk(dn::upsample_concat(low.x, skip.x, cat.x, n, h >> (l + 1), w >> (l + 1), low.c, skip.c, st));
         prev = idx++;
-        chk(conv_fwd(conv++, act_[prev], act_[idx].x, nullptr, st, nullptr, infer));
+        chk(conv_fwd(conv++, act_[prev], act_[idx].x, nullptr, st, nullptr, fuse));
         prev = idx++;
         dn::TcFuse f;
         const bool up = fuse && l > 0;
         if (up) f.cat = act_[kCat[l - 1]].x, f.cat_c = act_[kCat[l - 1]].c, f.cat_up = 1;
         chk(conv_fwd(conv++, act_[prev], up && infer ? nullptr : act_[idx].x, nullptr, st, up ? &f : nullptr,
-                     infer));
+                     fuse));
         prev = idx++;
     }
     // output convolution (no ReLU), FP32; the network predicts a correction
@@ -368,7 +369,7 @@ cudaError_t Denoiser::forward(const float *rad, const __half *feat, int n, int h
         dn::TcFuse f;
         f.res = x0, f.res_c = x0_c;
         f.rad = out_rad, f.feat = feat;
-        chk(conv_fwd(conv, act_[prev], nullptr, out_, st, &f, infer));
+        chk(conv_fwd(conv, act_[prev], nullptr, out_, st, &f, fuse));
     } else {
         chk(conv_fwd(conv, act_[prev], nullptr, out_, st));
         chk(dn::add_input(out_, x0, x0_c, px, st));
@@ -419,7 +420,11 @@ cudaError_t Denoiser::backward(const float *target, cudaStream_t st) {
                     return;
                 }
             }
-            chk(dn::conv3x3_forward_tc(pl, wtcb_ + tcb_off_[ci], zero_bias_, nullptr, in.g, partial_, err_, st));
+            // programmatic launch: its prologue loads the transposed weights
+            // (packed after the last optimizer step) while the bias
+            // gradient's final sums (the last kernel of grad_prep) run
+            chk(dn::conv3x3_forward_tc(pl, wtcb_ + tcb_off_[ci], zero_bias_, nullptr, in.g, partial_, err_, st,
+                                       nullptr, true));
         }
         dn::TcWgradPlan &wg = plans_wg_[ci];
         if (wg.g != gb16_ || wg.n != n || wg.h != hh || wg.w != ww) {

@@ -218,6 +218,8 @@ __global__ void k_grad_prep(const __nv_bfloat16 *y, const float *g, __nv_bfloat1
 // t, t + 256, ..., then a fixed tree adds the 256 sums (the same order on
 // every run).
 __global__ void k_bias_finalize(const float *part, float *db, int blocks, int c) {
+    // a backward-data convolution launched next may start its prologue now
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     __shared__ float sm[256];
     const int k = (int)blockIdx.x, t = (int)threadIdx.x;
     float s = 0.f;

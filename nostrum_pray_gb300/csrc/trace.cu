@@ -45,8 +45,14 @@ __global__ void __launch_bounds__(128) k_trace_closest(DevScene s, const float *
 // whose colour saturated stops casting (the reference's early break).
 // kPrimPacket / kShadowPacket: the warp traverses its tile's primary /
 // occlusion rays as a packet (traverse_coherent).
+// Resident blocks per SM (the register cap): the all-packet walk (one
+// shared-memory stack per warp) gains from more warps in flight despite
+// some spills (1.31M sphere: 8 / 9 / 10 blocks 1.660 / 1.626 /
+// 1.616 ms per frame); per-lane and primary-packet walks lose from them.
+constexpr int kPacketBlocks = 10;
+
 template <bool kCount, int kStackN, bool kPrimPacket, bool kShadowPacket>
-__global__ void __launch_bounds__(128, 8) k_render_rt(DevScene s, RtLaunch L) {
+__global__ void __launch_bounds__(128, kShadowPacket ? kPacketBlocks : 8) k_render_rt(DevScene s, RtLaunch L) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t px, py;
     const bool active = pixel_of(i, L.cam.width, L.cam.height, px, py);
