@@ -166,6 +166,15 @@ pray_status pray_scene_stats(const pray_scene *s, uint64_t *out);
 pray_status pray_trace_closest(pray_scene *s, const float *rays_dev, uint64_t n, float det_epsilon,
                                int32_t *ids_dev, float *t_dev, void *stream);
 
+/* Occlusion (shadow) rays: occluded_dev[i] = 1 iff some triangle is hit at
+ * distance t > 0 with t * t < dist2_dev[i], else 0; the walk stops at the
+ * first such triangle. The same answer as the reference's shadow test, the
+ * closest hit followed by lightDistSq > dst * dst (src/pray.cpp:39-43);
+ * dist2 <= 0 gives 0. rays_dev: n x 9 floats as for pray_trace_closest; all
+ * device pointers. */
+pray_status pray_trace_occluded(pray_scene *s, const float *rays_dev, const float *dist2_dev, uint64_t n,
+                                float det_epsilon, uint8_t *occluded_dev, void *stream);
+
 /* pray_trace_closest for rays in host memory, for host code that asks the
  * spatial database one ray or one batch at a time
  * (SpatialDatabase::intersect(const Ray&, Triangle&, float&),

@@ -654,6 +654,17 @@ pray_status pray_trace_closest(pray_scene *s, const float *rays, uint64_t n, flo
     return PRAY_OK;
 }
 
+pray_status pray_trace_occluded(pray_scene *s, const float *rays, const float *dist2, uint64_t n, float eps,
+                                uint8_t *occluded, void *stream) {
+    if (!s || (n > 0 && (!rays || !dist2 || !occluded))) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n >= (1ull << 40)) return set_error(PRAY_ERR_INVALID_ARGUMENT, "too many rays");
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
+    e = launch_trace_occluded(s->view(), rays, dist2, n, eps, occluded, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_error(e, "trace_occluded launch");
+    return PRAY_OK;
+}
+
 pray_status pray_trace_closest_host(pray_scene *s, const float *rays_host, uint64_t n, float eps, int32_t *ids_host,
                                     float *t_host) {
     if (!s || (n > 0 && (!rays_host || !ids_host || !t_host))) return set_error(PRAY_ERR_INVALID_ARGUMENT, "NULL argument");

@@ -100,7 +100,7 @@ cudaError_t Denoiser::init(uint64_t seed) {
         (e = take(wb_, total)) != cudaSuccess || (e = take(wtc_, tc_total)) != cudaSuccess ||
         (e = take(wtcb_, tcb_total)) != cudaSuccess || (e = take(zero_bias_, 256)) != cudaSuccess ||
         (e = cudaMemset(zero_bias_, 0, 256 * sizeof(float))) != cudaSuccess ||
-        (e = take(loss_, 1)) != cudaSuccess || (e = take(err_, 1)) != cudaSuccess ||
+        (e = take(loss_, 1 + dn::kL1Parts)) != cudaSuccess || (e = take(err_, 1)) != cudaSuccess ||
         (e = cudaMemset(err_, 0, sizeof(int))) != cudaSuccess)
         return e;
     // He-normal weights, zero biases, from the seed
@@ -384,10 +384,9 @@ cudaError_t Denoiser::backward(const float *target, cudaStream_t st) {
     cudaError_t e = cudaSuccess;
     auto chk = [&](cudaError_t x) { if (x != cudaSuccess && e == cudaSuccess) e = x; };
     chk(cudaMemsetAsync(g_, 0, n_params_ * 4, st));
-    chk(cudaMemsetAsync(loss_, 0, 4, st));
     for (Buf &b : act_)
         if (b.g) chk(cudaMemsetAsync(b.g, 0, (size_t)n * (h >> b.level) * (w >> b.level) * b.c * 4, st));
-    chk(dn::l1_loss(out_, target, feat_, gout_, loss_, px * 3, st));
+    chk(dn::l1_loss(out_, target, feat_, gout_, loss_, loss_ + 1, px * 3, st));
     // input gradient (when need_dx) and weight / bias gradients of convolution
     // ci from its output gradient g, masked by the ReLU of its output y (NULL:
     // no ReLU). With the tensor cores the input gradient is a forward

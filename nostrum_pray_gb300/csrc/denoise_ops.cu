@@ -331,9 +331,11 @@ __global__ void k_pack_input(const float *rad, const __half *feat, __nv_bfloat16
 }
 
 // L1 loss on log1p(radiance / demodulation): out = network output (log
-// space), target in linear radiance; loss sum into loss[0], gradient into g
-// (scaled by 1/n)
-__global__ void k_l1(const float *out, const float *target, const __half *feat, float *g, float *loss, size_t n) {
+// space), target in linear radiance; gradient into g (scaled by 1/n), each
+// block's sum of |d| into part[block] by a fixed tree; k_l1_finalize adds the
+// blocks' sums in a fixed order, so the loss is the same bits on every run
+__global__ void k_l1(const float *out, const float *target, const __half *feat, float *g, float *part, size_t n) {
+    __shared__ float sm[256];
     float acc = 0.f;
     const float inv = 1.f / (float)n;
     for (size_t i = gtid(); i < n; i += gstride()) {
@@ -341,8 +343,26 @@ __global__ void k_l1(const float *out, const float *target, const __half *feat, 
         acc += fabsf(d);
         g[i] = (d > 0.f ? 1.f : (d < 0.f ? -1.f : 0.f)) * inv;
     }
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc * inv);
+    sm[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sm[0];
+}
+
+__global__ void k_l1_finalize(const float *part, int blocks, float *loss, float inv) {
+    __shared__ float sm[256];
+    float s = 0.f;
+    for (int b = (int)threadIdx.x; b < blocks; b += 256) s += part[b];
+    sm[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) loss[0] = sm[0] * inv;
 }
 
 // residual output: out (log space) += the input's log(1 + radiance) channels
@@ -395,7 +415,9 @@ __global__ void k_to_bf16(const float *a, __nv_bfloat16 *b, size_t n) {
     for (size_t i = gtid(); i < n; i += gstride()) b[i] = __float2bfloat16(a[i]);
 }
 
-unsigned blocks_for(size_t n) { return (unsigned)std::min<size_t>((n + 255) / 256, 152 * 32); }
+constexpr size_t kMaxBlocks = 152 * 32;  // grid-stride kernels: at most this many blocks of 256
+static_assert(kL1Parts >= (int)kMaxBlocks, "l1_loss scratch holds one sum per block");
+unsigned blocks_for(size_t n) { return (unsigned)std::min<size_t>((n + 255) / 256, kMaxBlocks); }
 
 }  // namespace
 
@@ -478,9 +500,11 @@ cudaError_t pack_input(const float *rad, const __half *feat, __nv_bfloat16 *x, _
     k_pack_input<<<blocks_for(pixels), 256, 0, st>>>(rad, feat, x, x16, pixels);
     return cudaGetLastError();
 }
-cudaError_t l1_loss(const float *out, const float *target, const __half *feat, float *g, float *loss, size_t n,
-                    cudaStream_t st) {
-    k_l1<<<blocks_for(n), 256, 0, st>>>(out, target, feat, g, loss, n);
+cudaError_t l1_loss(const float *out, const float *target, const __half *feat, float *g, float *loss, float *part,
+                    size_t n, cudaStream_t st) {
+    const unsigned blocks = blocks_for(n);
+    k_l1<<<blocks, 256, 0, st>>>(out, target, feat, g, part, n);
+    k_l1_finalize<<<1, 256, 0, st>>>(part, (int)blocks, loss, 1.f / (float)n);
     return cudaGetLastError();
 }
 cudaError_t add_input(float *out, const __nv_bfloat16 *x0, int x0_c, size_t pixels, cudaStream_t st) {

@@ -135,8 +135,11 @@ cudaError_t pack_input(const float *rad, const __half *feat, __nv_bfloat16 *x, _
 // cat = [nearest 2x upsampling of low (c channels, h x w), skip (cs channels)]
 cudaError_t upsample_concat(const __nv_bfloat16 *low, const __nv_bfloat16 *skip, __nv_bfloat16 *cat, int n, int h,
                             int w, int c, int cs, cudaStream_t st);
-cudaError_t l1_loss(const float *out, const float *target, const __half *feat, float *g, float *loss, size_t n,
-                    cudaStream_t st);
+// L1 loss (mean over the n values, into loss[0]) and its gradient; part:
+// scratch of kL1Parts floats (per-block sums, added in a fixed order)
+constexpr int kL1Parts = 152 * 32;
+cudaError_t l1_loss(const float *out, const float *target, const __half *feat, float *g, float *loss, float *part,
+                    size_t n, cudaStream_t st);
 // out (3 channels) += the first 3 of x0's x0_c channels (the input's log radiance)
 cudaError_t add_input(float *out, const __nv_bfloat16 *x0, int x0_c, size_t pixels, cudaStream_t st);
 cudaError_t expm1_out(const float *out, const __half *feat, float *rad, size_t n, cudaStream_t st);

@@ -18,6 +18,29 @@ namespace {
 
 using namespace dev;
 
+// Occlusion of caller-given rays: 1 iff some triangle is hit at t > 0 with
+// t^2 < dist2 (the any-hit walk stops at the first such triangle). The
+// reference asks for the closest hit and tests lightDistSq > dst * dst
+// (src/pray.cpp:39-43); the closest t satisfies it iff some t does.
+__global__ void __launch_bounds__(128) k_trace_occluded(DevScene s, const float *__restrict__ rays,
+                                                        const float *__restrict__ dist2, uint64_t n, float eps,
+                                                        uint8_t *__restrict__ occluded) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < n;
+    RayF r{};
+    float d2 = 0.f;
+    if (valid) {
+        const float *p = rays + 9 * i;
+        r.ox = p[0], r.oy = p[1], r.oz = p[2];
+        r.dx = p[3], r.dy = p[4], r.dz = p[5];
+        r.ix = p[6], r.iy = p[7], r.iz = p[8];
+        d2 = dist2[i];
+    }
+    float t;
+    const int pos = traverse<true>(s, r, eps, d2, valid && s.n_refs > 0 && d2 > 0.f, t);
+    if (valid) occluded[i] = pos >= 0 ? 1 : 0;
+}
+
 __global__ void __launch_bounds__(128) k_trace_closest(DevScene s, const float *__restrict__ rays, uint64_t n,
                                                        float eps, int32_t *__restrict__ ids,
                                                        float *__restrict__ ts) {
@@ -174,6 +197,15 @@ __global__ void __launch_bounds__(128) k_features(DevScene s, CameraConsts cam, 
 cudaError_t launch_features(const DevScene &s, const CameraConsts &cam, float eps, __half *out, cudaStream_t stream) {
     const uint64_t threads = warp_tiles(cam.width, cam.height) * 32;
     k_features<<<(unsigned)((threads + 127) / 128), 128, 0, stream>>>(s, cam, eps, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_occluded(const DevScene &s, const float *rays, const float *dist2, uint64_t n, float eps,
+                                  uint8_t *occluded, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    const unsigned threads = 128;
+    const uint64_t blocks = (n + threads - 1) / threads;
+    k_trace_occluded<<<(unsigned)blocks, threads, 0, stream>>>(s, rays, dist2, n, eps, occluded);
     return cudaGetLastError();
 }
 

@@ -91,6 +91,8 @@ cudaError_t launch_relmse(const double *img, double img_scale, const double *ref
 
 cudaError_t launch_features(const DevScene &s, const CameraConsts &cam, float eps, __half *out, cudaStream_t stream);
 
+cudaError_t launch_trace_occluded(const DevScene &s, const float *rays, const float *dist2, uint64_t n, float eps,
+                                  uint8_t *occluded, cudaStream_t stream);
 cudaError_t launch_trace_closest(const DevScene &s, const float *rays, uint64_t n, float eps, int32_t *ids,
                                  float *ts, cudaStream_t stream);
 

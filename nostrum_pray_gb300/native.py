@@ -73,7 +73,7 @@ EXPORTED = [
     "pray_host_tree_destroy", "pray_host_tree_stats", "pray_host_tree_dump", "pray_host_tree_precompute",
     "pray_host_tree_device_layout",
     "pray_camera", "pray_scene_create", "pray_scene_destroy", "pray_scene_stats", "pray_scene_set_traversal",
-    "pray_scene_traversal", "pray_trace_closest", "pray_trace_closest_host",
+    "pray_scene_traversal", "pray_trace_closest", "pray_trace_closest_host", "pray_trace_occluded",
     "pray_render_rt", "pray_render_rt_host", "pray_render_rt_counts", "pray_render_pt", "pray_render_pt_host",
     "pray_accumulate_pt", "pray_relmse", "pray_render_pt_noalloc",
     "pray_batch_create", "pray_batch_destroy", "pray_batch_set_config", "pray_batch_tune", "pray_batch_render",
@@ -106,6 +106,7 @@ def lib():
         L.pray_scene_set_traversal.argtypes = [_vp, _i32]
         L.pray_scene_traversal.argtypes = [_vp, ctypes.POINTER(_i32)]
         L.pray_trace_closest.argtypes = [_vp, _vp, _u64, _f32, _vp, _vp, _vp]
+        L.pray_trace_occluded.argtypes = [_vp, _vp, _vp, _u64, _f32, _vp, _vp]
         L.pray_trace_closest_host.argtypes = [_vp, _vp, _u64, _f32, _vp, _vp]
         L.pray_render_rt.argtypes = [_vp, ctypes.POINTER(RtParams), _vp, _vp, _vp, _vp, _vp]
         L.pray_render_rt_host.argtypes = [_vp, ctypes.POINTER(RtParams), _vp, _vp]
@@ -289,6 +290,12 @@ class Scene:
     def trace_closest(self, rays, det_eps: float, ids, ts, stream=None) -> None:
         n = rays.numel() // 9
         check(lib().pray_trace_closest(self._h, _ptr(rays), n, det_eps, _ptr(ids), _ptr(ts), _stream(stream)))
+
+    def trace_occluded(self, rays, dist2, det_eps: float, occluded, stream=None) -> None:
+        """occluded (uint8, n): 1 iff a triangle is hit at t > 0 with t^2 < dist2."""
+        n = rays.numel() // 9
+        check(lib().pray_trace_occluded(self._h, _ptr(rays), _ptr(dist2), n, det_eps, _ptr(occluded),
+                                        _stream(stream)))
 
     def trace_closest_host(self, rays: np.ndarray, det_eps: float) -> Tuple[np.ndarray, np.ndarray]:
         """Closest hits of host rays (n x 9 float32): (ids int32, distances float32)."""

@@ -72,6 +72,18 @@ def test_gradients_match_fp64_oracle(oracle, tensor_cores):
     assert off == den.num_params
 
 
+def test_gradients_deterministic():
+    """Loss and every gradient are the same bits on every call (fixed-order
+    reductions throughout, no floating-point atomics)."""
+    den = native.Denoiser(seed=6)
+    rad, feat, tgt = random_batch(2, 2, 80, 48)
+    t = lambda a: torch.from_numpy(a).cuda()
+    runs = [den.gradients(t(rad), t(feat), t(tgt)) for _ in range(3)]
+    for loss, g in runs[1:]:
+        assert loss == runs[0][0]
+        assert np.array_equal(g.view(np.uint32), runs[0][1].view(np.uint32))
+
+
 def test_training_reduces_loss():
     den = native.Denoiser(seed=2)
     rad, feat, tgt = random_batch(3, 4, 32, 32)

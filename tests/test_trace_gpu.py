@@ -163,6 +163,48 @@ def test_random_rays_inside_scene(oracle):
         np.testing.assert_array_equal(ts.view(np.uint32), wt.view(np.uint32))
 
 
+@pytest.mark.parametrize("tree", ["median", "sah"])
+def test_occlusion_rays(oracle, tree):
+    """pray_trace_occluded against the reference's shadow test on the
+    oracle's closest hits (occluded iff a hit with dist2 > t * t,
+    src/pray.cpp:39-43): random rays inside the soup with distances around
+    their closest hits, including dist2 exactly t * t (not occluded), the
+    next float above it (occluded), zero, negative and infinite."""
+    m = scenes.soup(10_000, 6)
+    st = scenes.soup_setup()
+    st.tree = tree
+    sc = native.Scene.from_setup(m, st)
+    orc = oracle.OracleScene.from_setup(m, st)
+    rng = np.random.default_rng(3)
+    n = 120_000
+    o = rng.uniform(-0.2, 1.2, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d[: n // 20, 1:] = 0.0
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    with np.errstate(divide="ignore"):
+        inv = (1.0 / d).astype(np.float32)
+    rays = np.concatenate([o, d, inv], 1).astype(np.float32)
+    for eps in (1e-4, 0.0):
+        wid, wt = orc.trace(rays, eps)
+        hit = wid >= 0
+        tt = np.where(hit, wt, 1.0).astype(np.float32)
+        t2 = (tt * tt).astype(np.float32)
+        kind = rng.integers(0, 7, n)
+        dist2 = np.select([kind == 0, kind == 1, kind == 2, kind == 3, kind == 4, kind == 5],
+                          [t2, np.nextafter(t2, np.float32(np.inf)), np.float32(0), np.float32(-1),
+                           np.float32(np.inf), t2 * np.float32(0.25)],
+                          rng.uniform(0, 4, n).astype(np.float32) * t2).astype(np.float32)
+        want = (hit & (dist2 > t2)).astype(np.uint8)
+        r = torch.from_numpy(rays).cuda()
+        dd = torch.from_numpy(dist2).cuda()
+        occ = torch.empty(n, dtype=torch.uint8, device="cuda")
+        sc.trace_occluded(r, dd, eps, occ)
+        torch.cuda.synchronize()
+        got = occ.cpu().numpy()
+        assert int((got != want).sum()) == 0, f"{int((got != want).sum())} occlusion answers differ"
+        assert 0 < int(want.sum()) < n
+
+
 def test_ties_duplicated_triangles(oracle):
     """Coincident copies of each triangle: equal distances, so the first in
     the reference's depth-first order must win."""
