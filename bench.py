@@ -699,6 +699,11 @@ def run_denoise_infer(args):
     intensity = flops / nbytes
     ridge = peak * 1e12 / (hbm * 1e9)
     gbs = nbytes / per / 1e9
+    # DRAM bytes of one pass from the committed ncu capture (the sum over the
+    # pass's launches, one 512^2 frame on the tensor cores), scaled by frames
+    prof = committed_profile("denoise_infer", f"{res}")  # profiles/denoise_infer_512.json
+    traffic = (int(prof["dram_bytes_per_frame"] * nb) if prof.get("dram_bytes_per_frame") and not args.dn_cuda_cores
+               else None)
     line = {"metric": "denoised frames/s", "value": round(nb * args.steps / (ms / 1e3), 2), "unit": "frames/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
@@ -717,7 +722,7 @@ def run_denoise_infer(args):
                          if intensity < ridge else
                          {"bound": "tensor", "achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s",
                           "frac": round(achieved / peak, 5), "peak_kind": peak_kind})
-                        | {"traffic": None, "algorithmic_bytes_per_call": nbytes, "algorithmic_flops_per_call": flops,
+                        | {"traffic": traffic, "algorithmic_bytes_per_call": nbytes, "algorithmic_flops_per_call": flops,
                            "intensity_flop_per_byte": round(intensity, 1), "ridge_flop_per_byte": round(ridge, 1),
                            "tensor": {"achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s",
                                       "frac": round(achieved / peak, 5), "peak_kind": peak_kind},

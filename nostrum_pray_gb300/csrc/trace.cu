@@ -22,6 +22,7 @@ using namespace dev;
 // t^2 < dist2 (the any-hit walk stops at the first such triangle). The
 // reference asks for the closest hit and tests lightDistSq > dst * dst
 // (src/pray.cpp:39-43); the closest t satisfies it iff some t does.
+template <int kStackN>
 __global__ void __launch_bounds__(128) k_trace_occluded(DevScene s, const float *__restrict__ rays,
                                                         const float *__restrict__ dist2, uint64_t n, float eps,
                                                         uint8_t *__restrict__ occluded) {
@@ -37,10 +38,11 @@ __global__ void __launch_bounds__(128) k_trace_occluded(DevScene s, const float 
         d2 = dist2[i];
     }
     float t;
-    const int pos = traverse<true>(s, r, eps, d2, valid && s.n_refs > 0 && d2 > 0.f, t);
+    const int pos = traverse<true, false, kStackN>(s, r, eps, d2, valid && s.n_refs > 0 && d2 > 0.f, t);
     if (valid) occluded[i] = pos >= 0 ? 1 : 0;
 }
 
+template <int kStackN>
 __global__ void __launch_bounds__(128) k_trace_closest(DevScene s, const float *__restrict__ rays, uint64_t n,
                                                        float eps, int32_t *__restrict__ ids,
                                                        float *__restrict__ ts) {
@@ -54,7 +56,7 @@ __global__ void __launch_bounds__(128) k_trace_closest(DevScene s, const float *
         r.ix = p[6], r.iy = p[7], r.iz = p[8];
     }
     float t;
-    const int pos = traverse<false>(s, r, eps, 0.f, valid && s.n_refs > 0, t);
+    const int pos = traverse<false, false, kStackN>(s, r, eps, 0.f, valid && s.n_refs > 0, t);
     if (valid) {
         ids[i] = pos >= 0 ? (int32_t)__float_as_uint(__ldg(&s.tris[pos].v0[3])) : -1;
         ts[i] = t;
@@ -205,7 +207,11 @@ cudaError_t launch_trace_occluded(const DevScene &s, const float *rays, const fl
     if (n == 0) return cudaSuccess;
     const unsigned threads = 128;
     const uint64_t blocks = (n + threads - 1) / threads;
-    k_trace_occluded<<<(unsigned)blocks, threads, 0, stream>>>(s, rays, dist2, n, eps, occluded);
+    // a 32-entry stack (half the per-thread local memory) when the hierarchy is shallow enough
+    if (s.depth < 32)
+        k_trace_occluded<32><<<(unsigned)blocks, threads, 0, stream>>>(s, rays, dist2, n, eps, occluded);
+    else
+        k_trace_occluded<kStack><<<(unsigned)blocks, threads, 0, stream>>>(s, rays, dist2, n, eps, occluded);
     return cudaGetLastError();
 }
 
@@ -214,7 +220,10 @@ cudaError_t launch_trace_closest(const DevScene &s, const float *rays, uint64_t 
     if (n == 0) return cudaSuccess;
     const unsigned threads = 128;
     const uint64_t blocks = (n + threads - 1) / threads;
-    k_trace_closest<<<(unsigned)blocks, threads, 0, stream>>>(s, rays, n, eps, ids, ts);
+    if (s.depth < 32)
+        k_trace_closest<32><<<(unsigned)blocks, threads, 0, stream>>>(s, rays, n, eps, ids, ts);
+    else
+        k_trace_closest<kStack><<<(unsigned)blocks, threads, 0, stream>>>(s, rays, n, eps, ids, ts);
     return cudaGetLastError();
 }
 
