@@ -25,7 +25,7 @@ constexpr uint32_t kLeafFlag = 0x80000000u;
 constexpr int kMaxTreeDepth = 30;        // deepest reference tree the API accepts
 constexpr int kMaxTraversalDepth = 62;   // deepest device hierarchy (reference tree + leaf refinement)
 
-struct alignas(16) GNode {
+struct alignas(32) GNode {  // 32-byte aligned: one 256-bit load per node (traverse.cuh ldg_node)
     float lo[3];
     uint32_t a;
     float hi[3];
