@@ -43,9 +43,14 @@ struct FrameSrc {
 // kRefill (mode 1): a persistent grid whose lanes take pixels from the
 // frame's counter (512^2 at 1 spp: 1.68 -> 1.49 ms; room 1024^2 at 64 spp
 // unchanged). Mode 0 keeps one pixel per lane: refilled, it measured 6 %
-// slower on the room.
-template <bool kRefill>
-__global__ void __launch_bounds__(128, 10) k_render_pt(DevScene s, PtLaunch L) {
+// slower on the room. kBlocks: resident blocks per SM (the register cap).
+// Long frames run 10 (48 registers); a frame of fewer paths than two rounds
+// of those lanes is bound by its last paths, which run faster with more
+// registers and fewer spills: 8 blocks (64 registers) take 512^2 at 1 spp
+// from 1.231 to 1.186 ms, where the 1024^2 x 64-spp room drops from 200.2
+// to 191.0 Msamples/s.
+template <bool kRefill, int kBlocks>
+__global__ void __launch_bounds__(128, kBlocks) k_render_pt(DevScene s, PtLaunch L) {
     constexpr unsigned kFull = 0xFFFFFFFFu;
     uint32_t segments = 0, pixels = 0;
     if (kRefill) {
@@ -92,11 +97,18 @@ cudaError_t launch_render_pt(const DevScene &s, const PtLaunch &L, int sm_count,
         k_render_pt_diffuse<<<(unsigned)blocks, bs, 0, stream>>>(s, L);
     } else if (L.mode == 1) {
         if (!L.next_pixel) return cudaErrorInvalidValue;
-        // persistent: as many blocks as stay resident (10 per SM), or fewer
-        const uint64_t resident = (uint64_t)(sm_count > 0 ? sm_count : 1) * 10;
-        k_render_pt<true><<<(unsigned)(blocks < resident ? blocks : resident), bs, 0, stream>>>(s, L);
+        // persistent: as many blocks as stay resident, or fewer
+        const uint64_t sms = (uint64_t)(sm_count > 0 ? sm_count : 1);
+        const uint64_t paths = (uint64_t)L.cam.width * L.cam.height * L.num_samples;
+        if (paths < 2 * sms * 10 * bs) {
+            const uint64_t resident = sms * 8;
+            k_render_pt<true, 8><<<(unsigned)(blocks < resident ? blocks : resident), bs, 0, stream>>>(s, L);
+        } else {
+            const uint64_t resident = sms * 10;
+            k_render_pt<true, 10><<<(unsigned)(blocks < resident ? blocks : resident), bs, 0, stream>>>(s, L);
+        }
     } else {
-        k_render_pt<false><<<(unsigned)blocks, bs, 0, stream>>>(s, L);
+        k_render_pt<false, 10><<<(unsigned)blocks, bs, 0, stream>>>(s, L);
     }
     return cudaGetLastError();
 }
