@@ -74,10 +74,14 @@ __global__ void __launch_bounds__(128) k_trace_closest(DevScene s, const float *
 // shared-memory stack per warp) gains from more warps in flight despite
 // some spills (1.31M sphere: 8 / 9 / 10 blocks 1.660 / 1.626 /
 // 1.616 ms per frame); per-lane and primary-packet walks lose from them.
-constexpr int kPacketBlocks = 10;
+// Smaller blocks, so that a warp's slot frees without waiting for the
+// block's other warps, measured slower: 64 x 20 1.68 ms, 32 x 32 1.63 ms,
+// 64 x 16 1.74 ms against 1.61 ms for 128 x 10.
+constexpr int kPacketBlocks = 10, kPacketThreads = 128;
 
 template <bool kCount, int kStackN, bool kPrimPacket, bool kShadowPacket>
-__global__ void __launch_bounds__(128, kShadowPacket ? kPacketBlocks : 8) k_render_rt(DevScene s, RtLaunch L) {
+__global__ void __launch_bounds__(kShadowPacket ? kPacketThreads : 128, kShadowPacket ? kPacketBlocks : 8)
+    k_render_rt(DevScene s, RtLaunch L) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t px, py;
     const bool active = pixel_of(i, L.cam.width, L.cam.height, px, py);
@@ -231,7 +235,7 @@ cudaError_t launch_render_rt(const DevScene &s, const RtLaunch &L, cudaStream_t 
     const uint64_t tiles = warp_tiles(L.cam.width, L.cam.height);
     const uint64_t threads = tiles * 32;
     if (threads == 0) return cudaSuccess;
-    const unsigned bs = 128, grid = (unsigned)((threads + bs - 1) / bs);
+    const unsigned bs = L.packets == 1 ? kPacketThreads : 128, grid = (unsigned)((threads + bs - 1) / bs);
     // a 32-entry stack (half the per-thread local memory) when the hierarchy is shallow enough
     const bool small = s.depth < 32;
     auto go = [&](auto kernel) { kernel<<<grid, bs, 0, stream>>>(s, L); };
