@@ -112,6 +112,10 @@ struct pray_scene {
     uint64_t wf_capacity = 0, wf_pixels = 0;
     cudaStream_t wf_stream = nullptr;
     cudaEvent_t wf_ev_in = nullptr, wf_ev_out = nullptr;
+    // second stream and fork / join events of a recorded wavefront frame
+    // (each bounce's occlusion pass beside the next bounce's extend pass)
+    cudaStream_t wf_side = nullptr;
+    cudaEvent_t wf_fork = nullptr, wf_join = nullptr;
     cudaGraphExec_t wf_exec = nullptr;
     PtLaunch wf_key;
     uint64_t wf_key_cap = 0;
@@ -163,7 +167,11 @@ struct pray_scene {
         if (wf_stream) cudaStreamDestroy(wf_stream);
         if (wf_ev_in) cudaEventDestroy(wf_ev_in);
         if (wf_ev_out) cudaEventDestroy(wf_ev_out);
+        if (wf_side) cudaStreamDestroy(wf_side);
+        if (wf_fork) cudaEventDestroy(wf_fork);
+        if (wf_join) cudaEventDestroy(wf_join);
         d_wf = nullptr, wf_exec = nullptr, wf_stream = nullptr, wf_ev_in = nullptr, wf_ev_out = nullptr;
+        wf_side = nullptr, wf_fork = nullptr, wf_join = nullptr;
         wf_bytes = 0;
         d_nodes = nullptr, d_tris = nullptr, d_shade = nullptr, d_rgb = nullptr, d_counters = nullptr;
         d_emit = nullptr, d_emit_cdf = nullptr;
@@ -342,7 +350,10 @@ pray_status run_pt(pray_scene *s, const PtLaunch &L, int scheduler, uint32_t wav
     if (!s->wf_stream) {
         if ((e = cudaStreamCreateWithFlags(&s->wf_stream, cudaStreamNonBlocking)) != cudaSuccess ||
             (e = cudaEventCreateWithFlags(&s->wf_ev_in, cudaEventDisableTiming)) != cudaSuccess ||
-            (e = cudaEventCreateWithFlags(&s->wf_ev_out, cudaEventDisableTiming)) != cudaSuccess)
+            (e = cudaEventCreateWithFlags(&s->wf_ev_out, cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaStreamCreateWithFlags(&s->wf_side, cudaStreamNonBlocking)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&s->wf_fork, cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&s->wf_join, cudaEventDisableTiming)) != cudaSuccess)
             return cuda_error(e, "path-tracer stream set-up");
         int dev = 0;
         cudaGetDevice(&dev);
@@ -388,7 +399,8 @@ pray_status run_pt(pray_scene *s, const PtLaunch &L, int scheduler, uint32_t wav
         cudaGraph_t g = nullptr;
         if ((e = cudaStreamBeginCapture(s->wf_stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
             return cuda_error(e, "graph capture");
-        cudaError_t le = record_wavefront_frame(s->view(), L, w, s->sm_count, s->wf_stream);
+        cudaError_t le = record_wavefront_frame(s->view(), L, w, s->sm_count, s->wf_stream, s->wf_side, s->wf_fork,
+                                                s->wf_join);
         e = cudaStreamEndCapture(s->wf_stream, &g);
         if (le != cudaSuccess || e != cudaSuccess) {
             if (g) cudaGraphDestroy(g);

@@ -71,13 +71,17 @@ struct WavefrontScratch {
 uint64_t wavefront_scratch_bytes(uint64_t capacity, uint64_t pixels);
 // Carves a scratch block of wavefront_scratch_bytes() bytes (256-byte aligned base).
 WavefrontScratch wavefront_carve(void *base, uint64_t capacity, uint64_t pixels);
-// Enqueues one whole frame (all rounds) on `stream`; capturable in a graph.
 // Loads every kernel a wavefront frame may launch (both traversal-stack
 // variants) on the current device, so that no later frame triggers a lazy
 // module load.
 cudaError_t wavefront_preload_kernels();
+// Enqueues one whole frame (all rounds) on `stream`; capturable in a graph.
+// With `side`, `fork` and `join` (a second stream and two events), each
+// bounce's occlusion pass runs on `side` beside the next bounce's extend
+// pass; without them every pass runs on `stream` in order. The same image.
 cudaError_t record_wavefront_frame(const DevScene &s, const PtLaunch &L, const WavefrontScratch &w, int sm_count,
-                                   cudaStream_t stream);
+                                   cudaStream_t stream, cudaStream_t side = nullptr, cudaEvent_t fork = nullptr,
+                                   cudaEvent_t join = nullptr);
 
 // Allocation-free wavefront frame on the static scratch of
 // wavefront_noalloc.cu (why receives a message on a size or set-up error).

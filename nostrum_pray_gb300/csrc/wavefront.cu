@@ -87,6 +87,7 @@ __global__ void __launch_bounds__(kThreads) k_wf_init(PtLaunch L, WavefrontScrat
         w.counts[2] = 0;
         w.counts[3] = 0;
         w.counts[4] = 0;
+        w.counts[5] = 0;
     }
     for (uint64_t i = first_index(); i < n; i += grid_stride()) {
         const uint64_t pixel = i % P;
@@ -119,17 +120,17 @@ __device__ __forceinline__ uint32_t warp_fetch(uint32_t *counter, unsigned idle,
 // kRefillIdle of its lanes have finished their ray, gives those lanes the next
 // queue entries (one atomic per warp), so lanes do not idle until the
 // slowest ray of the warp is done. Work is handed out through counts[3]
-// (reset by the shade pass); counts[4], the occlusion pass's counter, is
-// reset here.
+// (reset by the shade pass). It also empties the next shade pass's output
+// queue and its occlusion-job count (counts[jobs]; the occlusion pass of the
+// previous bounce, which may run beside this one, reads the other slot).
 template <int kStackN>
 __global__ void __launch_bounds__(kThreads, kTraceBlocksPerSm) k_wf_extend(DevScene s, PtLaunch L, WavefrontScratch w,
-                                                                         int in, int out) {
+                                                                         int in, int out, int jobs) {
     constexpr unsigned kFull = 0xFFFFFFFFu;
     const uint32_t n = w.counts[in];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         w.counts[out] = 0;
-        w.counts[2] = 0;
-        w.counts[4] = 0;
+        w.counts[jobs] = 0;
     }
     uint32_t seg = 0;
     Trav T;
@@ -164,10 +165,14 @@ __global__ void __launch_bounds__(kThreads, kTraceBlocksPerSm) k_wf_extend(DevSc
     if (L.counters) warp_count(L.counters + 1, seg);
 }
 
+// Shading of every queued path: background or emitter, next-event job
+// (appended to counts[jobs]), cosine bounce and Russian roulette into the
+// queue `out`. Resets the fetch counters of the occlusion pass that follows
+// and of the next extend pass (counts[4], counts[3]).
 __global__ void __launch_bounds__(kThreads) k_wf_shade(DevScene s, PtLaunch L, WavefrontScratch w, int in, int out,
-                                                       uint32_t round_base, uint64_t P) {
+                                                       int jobs, uint32_t round_base, uint64_t P) {
     const uint32_t n = w.counts[in];
-    if (blockIdx.x == 0 && threadIdx.x == 0) w.counts[3] = 0;  // the next extend pass's fetch counter
+    if (blockIdx.x == 0 && threadIdx.x == 0) w.counts[3] = w.counts[4] = 0;
     for (uint64_t i = first_index(); i < rounded(n); i += grid_stride()) {
         bool cont = false, job = false;
         uint32_t p = 0;
@@ -253,7 +258,7 @@ __global__ void __launch_bounds__(kThreads) k_wf_shade(DevScene s, PtLaunch L, W
             }
             w.rad[p] = R;
         }
-        const uint32_t js = warp_append(w.counts + 2, job);
+        const uint32_t js = warp_append(w.counts + jobs, job);
         if (job) {
             float4 *j = w.shadow + 3ull * js;
             j[0] = jo;
@@ -265,13 +270,14 @@ __global__ void __launch_bounds__(kThreads) k_wf_shade(DevScene s, PtLaunch L, W
     }
 }
 
-// Any-hit test of every occlusion job, with the same dynamic fetch
-// (counts[4]); an unoccluded job adds its contribution to its path.
+// Any-hit test of every occlusion job (counts[jobs] of them), with the same
+// dynamic fetch (counts[4]); an unoccluded job adds its contribution to its
+// path.
 template <int kStackN>
 __global__ void __launch_bounds__(kThreads, kTraceBlocksPerSm) k_wf_occlude(DevScene s, PtLaunch L,
-                                                                          WavefrontScratch w) {
+                                                                          WavefrontScratch w, int jobs) {
     constexpr unsigned kFull = 0xFFFFFFFFu;
-    const uint32_t n = w.counts[2];
+    const uint32_t n = w.counts[jobs];
     uint32_t seg = 0;
     Trav T;
     TravStack<kStackN> S;
@@ -426,27 +432,42 @@ cudaError_t wavefront_preload_kernels() {
 }
 
 cudaError_t record_wavefront_frame(const DevScene &s, const PtLaunch &L, const WavefrontScratch &w, int sm_count,
-                                   cudaStream_t stream) {
+                                   cudaStream_t stream, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
     const uint64_t P = (uint64_t)L.cam.width * L.cam.height;
     if (P == 0 || L.num_samples == 0) return cudaSuccess;
     const uint32_t S = (uint32_t)std::min<uint64_t>(L.num_samples, std::max<uint64_t>(1, w.capacity / P));
     const unsigned grid = (unsigned)std::max(1, sm_count) * kTraceBlocksPerSm;
     const bool small_stack = s.depth < 32;  // a 32-entry traversal stack suffices
-    for (uint32_t base = 0; base < L.num_samples; base += S) {
+    // With a side stream, bounce b's occlusion pass runs there, beside bounce
+    // b + 1's extend pass (they touch different fields and counters: the
+    // two alternate occlusion-job counts, counts[2] and counts[5]), so each
+    // fills the other's ramp and tail; shade b + 1 waits for both.
+    const bool overlap = side && fork && join;
+    cudaError_t e = cudaSuccess;
+    for (uint32_t base = 0; base < L.num_samples && e == cudaSuccess; base += S) {
         const uint32_t Sr = std::min(S, L.num_samples - base);
         k_wf_init<<<grid, kThreads, 0, stream>>>(L, w, base, Sr, P);
-        for (uint32_t it = 0; it <= L.max_depth; it++) {
-            const int in = (int)(it & 1), out = 1 - in;
-            if (small_stack) k_wf_extend<32><<<grid, kThreads, 0, stream>>>(s, L, w, in, out);
-            else k_wf_extend<kStack><<<grid, kThreads, 0, stream>>>(s, L, w, in, out);
-            k_wf_shade<<<grid, kThreads, 0, stream>>>(s, L, w, in, out, base, P);
-            if (small_stack) k_wf_occlude<32><<<grid, kThreads, 0, stream>>>(s, L, w);
-            else k_wf_occlude<kStack><<<grid, kThreads, 0, stream>>>(s, L, w);
+        for (uint32_t it = 0; it <= L.max_depth && e == cudaSuccess; it++) {
+            const int in = (int)(it & 1), out = 1 - in, jobs = (it & 1) ? 5 : 2;
+            if (small_stack) k_wf_extend<32><<<grid, kThreads, 0, stream>>>(s, L, w, in, out, jobs);
+            else k_wf_extend<kStack><<<grid, kThreads, 0, stream>>>(s, L, w, in, out, jobs);
+            if (overlap && it > 0) e = cudaStreamWaitEvent(stream, join, 0);
+            k_wf_shade<<<grid, kThreads, 0, stream>>>(s, L, w, in, out, jobs, base, P);
+            cudaStream_t occ = stream;
+            if (overlap) {
+                if (e == cudaSuccess) e = cudaEventRecord(fork, stream);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(side, fork, 0);
+                occ = side;
+            }
+            if (small_stack) k_wf_occlude<32><<<grid, kThreads, 0, occ>>>(s, L, w, jobs);
+            else k_wf_occlude<kStack><<<grid, kThreads, 0, occ>>>(s, L, w, jobs);
+            if (overlap && e == cudaSuccess) e = cudaEventRecord(join, side);
         }
+        if (overlap && e == cudaSuccess) e = cudaStreamWaitEvent(stream, join, 0);
         k_wf_accumulate<<<grid, kThreads, 0, stream>>>(L, w, Sr, P, base == 0 ? 1 : 0);
     }
     k_wf_finish<<<grid, kThreads, 0, stream>>>(L, w, P);
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_relmse(const double *img, double a, const double *ref, double b, uint64_t n, double *out,
