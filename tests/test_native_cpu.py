@@ -176,6 +176,22 @@ def test_denoiser_table_matches_oracle(oracle):
     assert denoise.forward_flops(512, 512) == 47_563_407_360
 
 
+def test_denoiser_pass_accounting():
+    """Launches and algorithmic DRAM bytes of one inference pass. On the
+    tensor cores a 512^2 frame is input packing plus the 19 convolutions
+    (pooling, concatenation, residual and output transform are epilogue
+    stores); a 128^2 frame's output convolution splits its taps (a finalize
+    kernel) and so keeps the residual and output kernels; the CUDA-core pass
+    launches every kernel. Bytes: every tensor read and written once, 311.3
+    MB per 512^2 frame (157.5 MB read, 153.8 MB written), linear in frames."""
+    from nostrum_pray_gb300 import denoise
+    assert denoise.denoise_launches(512, 512) == 20
+    assert denoise.denoise_launches(512, 512, tensor_cores=False) == 30
+    assert denoise.denoise_launches(128, 128) == 1 + 19 + 1 + 2
+    assert denoise.forward_bytes(512, 512) == 311_296_000
+    assert denoise.forward_bytes(512, 512, 8) == 8 * 311_296_000
+
+
 def test_denoiser_fallback_sample_count():
     """The fallback render's sample count: the smallest count whose plain
     renders met the target on every calibration room, else the largest tried."""
