@@ -145,7 +145,10 @@ cudaError_t Denoiser::init(uint64_t seed) {
             cudaSuccess)
         return e;
     if ((e = dn::to_bf16(w_, wb_, total, 0)) != cudaSuccess) return e;
-    return refresh_tc_weights(0);
+    if ((e = refresh_tc_weights(0)) != cudaSuccess) return e;
+    // the converted and packed weights are in place before any stream
+    // (blocking or not) runs a pass with them
+    return cudaStreamSynchronize(0);
 }
 
 cudaError_t Denoiser::refresh_tc_weights(cudaStream_t st) {
@@ -156,7 +159,8 @@ cudaError_t Denoiser::set_params(const float *host) {
     cudaError_t e = cudaMemcpy(w_, host, n_params_ * 4, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return e;
     if ((e = dn::to_bf16(w_, wb_, n_params_, 0)) != cudaSuccess) return e;
-    return refresh_tc_weights(0);
+    if ((e = refresh_tc_weights(0)) != cudaSuccess) return e;
+    return cudaStreamSynchronize(0);
 }
 
 cudaError_t Denoiser::get_params(float *host) const {
